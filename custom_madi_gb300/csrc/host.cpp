@@ -1,0 +1,230 @@
+// Host-side native code: error plumbing and the geometry builders that run on
+// the CPU before any walk (KD tree of madi/ensemble.py:525-563 and the voxel
+// candidate grid used by the fp32 walker).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+#include "madi_host.h"
+
+namespace madi {
+namespace host {
+static thread_local char g_err[512] = {0};
+
+void clear_error() { g_err[0] = 0; }
+
+madi_status fail(madi_status code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+madi_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(MADI_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+}  // namespace host
+}  // namespace madi
+
+using namespace madi;
+
+extern "C" const char* madi_last_error_string(void) { return host::g_err; }
+extern "C" int32_t madi_abi_version(void) { return MADI_ABI_VERSION; }
+
+// ---------------------------------------------------------------------------
+// KD tree: each node takes the median (rank n/2) of its subset along the axis of
+// widest coordinate spread (first axis on ties); the lower-rank half becomes the
+// left subtree, the rest the right one; nodes are numbered in preorder.
+// ---------------------------------------------------------------------------
+namespace {
+struct KdBuilder {
+    const double* s;
+    int32_t *seed, *left, *right, *parent;
+    int8_t* axis;
+    int32_t next = 0;
+
+    int32_t build(int32_t* idx, int32_t n, int32_t up) {
+        if (n <= 0) return -1;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int32_t i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const double v = s[3 * (size_t)idx[i] + a];
+                lo[a] = std::min(lo[a], v);
+                hi[a] = std::max(hi[a], v);
+            }
+        int ax = 0;
+        for (int a = 1; a < 3; ++a)
+            if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
+        const int32_t mid = n / 2;
+        std::nth_element(idx, idx + mid, idx + n, [&](int32_t a, int32_t b) {
+            const double va = s[3 * (size_t)a + ax], vb = s[3 * (size_t)b + ax];
+            return va < vb || (va == vb && a < b);
+        });
+        const int32_t node = next++;
+        seed[node] = idx[mid];
+        axis[node] = (int8_t)ax;
+        parent[node] = up;
+        left[node] = build(idx, mid, node);
+        right[node] = build(idx + mid + 1, n - mid - 1, node);
+        return node;
+    }
+};
+}  // namespace
+
+extern "C" madi_status madi_kdtree_build(const double* seeds_xyz, int32_t n, int32_t* node_seed,
+                                         int8_t* node_axis, int32_t* node_left, int32_t* node_right,
+                                         int32_t* node_parent) {
+    host::clear_error();
+    if (n < 1 || !seeds_xyz || !node_seed || !node_axis || !node_left || !node_right || !node_parent)
+        return host::fail(MADI_ERR_INVALID, "kdtree_build: bad arguments");
+    std::vector<int32_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    KdBuilder b{seeds_xyz, node_seed, node_left, node_right, node_parent, node_axis};
+    const int32_t root = b.build(idx.data(), n, -1);
+    if (root != 0 || b.next != n) return host::fail(MADI_ERR_INVALID, "kdtree_build: inconsistent tree");
+    return MADI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Voxel candidate grid.  For voxel V (grown by eps) let
+//   D(V) = min over seeds s of the distance from s to the farthest point of V,
+// an upper bound of the nearest-seed distance d1(p) for every p in V.  A seed j
+// can (a) be nearest, (b) bind a facet (d_j < d1 + 2 alpha_1), or (c) have a
+// shifted facet within `cap` of p's label boundary only if
+//   dist(s_j, V) <= D(V) + 2 alpha_max + 2 cap,
+// because m_j >= (d_j - d1) / 2 for every seed.  Every such seed is listed.
+// ---------------------------------------------------------------------------
+namespace {
+struct Bins {
+    double lo[3], b;
+    int nb[3];
+    std::vector<int32_t> start, items;
+    int clampi(int v, int a) const { return std::min(std::max(v, 0), nb[a] - 1); }
+};
+
+Bins make_bins(const double* s, int32_t n, double b) {
+    Bins B;
+    double hi[3];
+    for (int a = 0; a < 3; ++a) { B.lo[a] = 1e300; hi[a] = -1e300; }
+    for (int32_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            B.lo[a] = std::min(B.lo[a], s[4 * (size_t)i + a]);
+            hi[a] = std::max(hi[a], s[4 * (size_t)i + a]);
+        }
+    B.b = b;
+    for (int a = 0; a < 3; ++a) B.nb[a] = std::max(1, (int)std::ceil((hi[a] - B.lo[a]) / b) + 1);
+    const size_t nbin = (size_t)B.nb[0] * B.nb[1] * B.nb[2];
+    std::vector<int32_t> cnt(nbin + 1, 0), which(n);
+    for (int32_t i = 0; i < n; ++i) {
+        int c[3];
+        for (int a = 0; a < 3; ++a) c[a] = B.clampi((int)std::floor((s[4 * (size_t)i + a] - B.lo[a]) / b), a);
+        which[i] = (int32_t)(((size_t)c[2] * B.nb[1] + c[1]) * B.nb[0] + c[0]);
+        cnt[which[i] + 1]++;
+    }
+    for (size_t k = 0; k < nbin; ++k) cnt[k + 1] += cnt[k];
+    B.start = cnt;
+    B.items.assign(n, 0);
+    std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+    for (int32_t i = 0; i < n; ++i) B.items[fill[which[i]]++] = i;
+    return B;
+}
+
+template <class F>
+void for_bins_in_box(const Bins& B, const double lo[3], const double hi[3], F f) {
+    int a0[3], a1[3];
+    for (int a = 0; a < 3; ++a) {
+        a0[a] = B.clampi((int)std::floor((lo[a] - B.lo[a]) / B.b), a);
+        a1[a] = B.clampi((int)std::floor((hi[a] - B.lo[a]) / B.b), a);
+    }
+    for (int z = a0[2]; z <= a1[2]; ++z)
+        for (int y = a0[1]; y <= a1[1]; ++y)
+            for (int x = a0[0]; x <= a1[0]; ++x) {
+                const size_t k = ((size_t)z * B.nb[1] + y) * B.nb[0] + x;
+                for (int32_t t = B.start[k]; t < B.start[k + 1]; ++t) f(B.items[t]);
+            }
+}
+}  // namespace
+
+extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h, double eps,
+                                       double safe_cap, uint32_t* offsets, void* ids, int32_t ids_u32,
+                                       int64_t capacity, int64_t* total) {
+    host::clear_error();
+    if (!seeds || n < 1 || G < 1 || !(h > 0.0) || eps < 0.0 || safe_cap < 0.0 || !total)
+        return host::fail(MADI_ERR_INVALID, "grid_build: bad arguments");
+    if (!ids_u32 && n > 65535) return host::fail(MADI_ERR_INVALID, "grid_build: uint16 ids need n <= 65535");
+    double amax = 0.0;
+    for (int32_t i = 0; i < n; ++i) amax = std::max(amax, seeds[4 * (size_t)i + 3]);
+    const double span = G * h;
+    const double spacing = std::cbrt(std::max(span * span * span, 1e-30) / std::max(n, 1));
+    const Bins B = make_bins(seeds, n, std::max(h, 0.5 * spacing));
+    std::vector<int32_t> list;
+    int64_t count = 0;
+    if (offsets) offsets[0] = 0;
+    for (int iz = 0; iz < G; ++iz)
+        for (int iy = 0; iy < G; ++iy)
+            for (int ix = 0; ix < G; ++ix) {
+                const double vlo[3] = {ix * h - eps, iy * h - eps, iz * h - eps};
+                const double vhi[3] = {(ix + 1) * h + eps, (iy + 1) * h + eps, (iz + 1) * h + eps};
+                const double c[3] = {0.5 * (vlo[0] + vhi[0]), 0.5 * (vlo[1] + vhi[1]), 0.5 * (vlo[2] + vhi[2])};
+                const double half_diag = 0.5 * std::sqrt(3.0) * (h + 2 * eps);
+                // nearest seed to the centre by growing search boxes
+                double best_c = 1e300;
+                for (double r = B.b;; r *= 2.0) {
+                    const double lo[3] = {c[0] - r, c[1] - r, c[2] - r}, hi[3] = {c[0] + r, c[1] + r, c[2] + r};
+                    for_bins_in_box(B, lo, hi, [&](int32_t j) {
+                        const double* q = seeds + 4 * (size_t)j;
+                        const double dx = q[0] - c[0], dy = q[1] - c[1], dz = q[2] - c[2];
+                        best_c = std::min(best_c, std::sqrt(dx * dx + dy * dy + dz * dz));
+                    });
+                    if (best_c <= r - B.b || r > 4.0 * (span + B.b * (B.nb[0] + B.nb[1] + B.nb[2]))) break;
+                }
+                // D(V): min over seeds of the farthest-corner distance; only seeds within
+                // best_c + half_diag of the centre can improve on the nearest one.
+                const double r1 = best_c + half_diag;
+                double D = 1e300;
+                {
+                    const double lo[3] = {c[0] - r1, c[1] - r1, c[2] - r1}, hi[3] = {c[0] + r1, c[1] + r1, c[2] + r1};
+                    for_bins_in_box(B, lo, hi, [&](int32_t j) {
+                        const double* q = seeds + 4 * (size_t)j;
+                        double acc = 0.0;
+                        for (int a = 0; a < 3; ++a) {
+                            const double e = std::max(std::fabs(q[a] - vlo[a]), std::fabs(q[a] - vhi[a]));
+                            acc += e * e;
+                        }
+                        D = std::min(D, std::sqrt(acc));
+                    });
+                }
+                const double R = (D + 2.0 * amax + 2.0 * safe_cap) * (1.0 + 1e-9) + 1e-9;
+                list.clear();
+                {
+                    const double lo[3] = {vlo[0] - R, vlo[1] - R, vlo[2] - R}, hi[3] = {vhi[0] + R, vhi[1] + R, vhi[2] + R};
+                    for_bins_in_box(B, lo, hi, [&](int32_t j) {
+                        const double* q = seeds + 4 * (size_t)j;
+                        double acc = 0.0;
+                        for (int a = 0; a < 3; ++a) {
+                            const double e = std::max(std::max(vlo[a] - q[a], q[a] - vhi[a]), 0.0);
+                            acc += e * e;
+                        }
+                        if (acc <= R * R) list.push_back(j);
+                    });
+                }
+                std::sort(list.begin(), list.end());
+                if (ids && count + (int64_t)list.size() <= capacity) {
+                    for (size_t t = 0; t < list.size(); ++t) {
+                        if (ids_u32) static_cast<uint32_t*>(ids)[count + t] = (uint32_t)list[t];
+                        else static_cast<uint16_t*>(ids)[count + t] = (uint16_t)list[t];
+                    }
+                }
+                count += (int64_t)list.size();
+                if (offsets) offsets[((size_t)iz * G + iy) * G + ix + 1] = (uint32_t)count;
+            }
+    *total = count;
+    if (count > 0xFFFFFFFFll) return host::fail(MADI_ERR_CAPACITY, "grid_build: more than 2^32 candidate ids");
+    if (ids && count > capacity) return host::fail(MADI_ERR_CAPACITY, "grid_build: capacity %lld < %lld ids",
+                                                   (long long)capacity, (long long)count);
+    return MADI_OK;
+}

@@ -1,0 +1,592 @@
+// GB300 walker: one persistent launch walks every (ensemble, p_p) job of a
+// batch.  Work unit = a tile of `tile_walkers` walkers (one per thread) of one
+// job; CTAs pull tiles from a device counter and stage the tile's geometry
+// (seeds + voxel candidate lists) into shared memory when it changes.
+//
+// Per step and walker (fp32 state, madi/walker_gpu.py:574-655 transition):
+//   propose x' = x + N(0, sigma^2 I)  (Philox4x32-10 + Box-Muller),
+//   boundary: fatal escape (SI) or periodic wrap,
+//   classify x' (Tier-1 proven safe sphere, else the voxel-grid rule, else fp64),
+//   m = endpoint membrane count, accept iff U64 < pp^m * 2^64, else revert,
+//   Y'(t) = int_0^t (x - x0) dt by the step trapezoid (fp32 within one storage
+//   interval, fp64 across intervals).
+// At the end the phase epilogue forms dM = Y(delta) + Y(Delta) - Y(Delta+delta)
+// per pair and axis and sums cos / sin(coef * u.dM) over the tile in exact
+// 64-bit fixed point.
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include "madi_device.cuh"
+#include "madi_host.h"
+
+namespace madi {
+
+// Per Y grid point: coefficient k_p in {-1, 0, 1, 2} of Y(t_j) in the pair-p
+// moment dM_p = Y(delta) + Y(Delta) - Y(Delta + delta), packed 2 bits per pair.
+struct Snap { uint32_t code, any; };
+MADI_DEV float snap_coef(uint32_t code, int p) { return (float)((int)((code >> (2 * p)) & 3u) - 1); }
+
+// Y relative to x0 -> the reference's origin L/2 (madi/walker_gpu.py:562-564).
+MADI_DEV double y_ref(double yrel, double x0, double half_L, double t) {
+    return yrel + (x0 - half_L) * t;
+}
+
+template <bool STAGED, int OUT, bool PERIODIC>
+__global__ void __launch_bounds__(256) walk_f32_kernel(const madi_walk_desc d) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_item;
+    const int nthr = blockDim.x;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int n_out = d.n_pairs * d.n_b * d.n_dirs;
+    // Dynamic shared memory: [stage][acc int64 x 2 n_out][occ u32 x n_grid][snap x n_grid]
+    unsigned char* stage = smem;
+    long long* acc = reinterpret_cast<long long*>(smem + d.stage_smem);
+    unsigned int* occ = reinterpret_cast<unsigned int*>(acc + 2 * n_out);
+    Snap* snap = reinterpret_cast<Snap*>(occ + d.n_grid);
+
+    for (int j = tid; j < d.n_grid; j += nthr) {
+        uint32_t code = 0, any = 0;
+        for (int p = 0; p < MADI_MAX_PAIRS; ++p) {
+            int k = 0;
+            if (p < d.n_pairs) k = (d.pair_jd[p] == j) + (d.pair_jD[p] == j) - (d.pair_js[p] == j);
+            code |= (uint32_t)(k + 1) << (2 * p);
+            any |= k != 0;
+        }
+        snap[j] = Snap{code, any};
+    }
+    int cur_geom = -1;
+    int first = 1;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            if (d.grid_blocks > 0) s_item = (int)atomicAdd(d.work_counter, 1u);
+            else s_item = first ? (int)blockIdx.x : d.n_tiles;
+        }
+        first = 0;
+        for (int i = tid; i < 2 * n_out; i += nthr) acc[i] = 0;
+        for (int j = tid; j < d.n_grid; j += nthr) occ[j] = 0;
+        __syncthreads();
+        const int item = s_item;
+        if (item >= d.n_tiles) break;
+        const int jn = find_job(d.jobs, d.n_jobs, item);
+        const madi_walk_job job = d.jobs[jn];
+        const madi_geometry gd = d.geoms[job.geom];
+        if (STAGED && job.geom != cur_geom) {
+            const uint4* src = reinterpret_cast<const uint4*>(gd.stage);
+            uint4* dst = reinterpret_cast<uint4*>(stage);
+            for (uint32_t i = tid; i < gd.stage_bytes / 16u; i += nthr) dst[i] = src[i];
+            cur_geom = job.geom;
+            __syncthreads();
+        }
+        const Geo g = make_geo(gd, STAGED ? stage : reinterpret_cast<const unsigned char*>(gd.stage));
+        const int local = (item - job.tile_begin) * nthr + tid;
+        const bool active = local < job.n_walkers;
+        const uint32_t widx = job.walker_base + (uint32_t)local;
+        const float L = (float)gd.L;
+        const float sigma = (float)d.sigma;
+        const bool cells = gd.has_cells != 0;
+        const bool stream = d.rng == MADI_RNG_STREAM;
+
+        // ---- initial position (Omega_src cube; the whole box when periodic) ----
+        float px = 0.f, py = 0.f, pz = 0.f;
+        double x0 = 0.0, y0 = 0.0, z0 = 0.0;
+        if (active) {
+            if (stream) {
+                x0 = d.init[3 * (size_t)local + 0];
+                y0 = d.init[3 * (size_t)local + 1];
+                z0 = d.init[3 * (size_t)local + 2];
+            } else {
+                const U4 r = philox10(U4{widx, 0u, 0u, 1u}, job.key0, job.key1);
+                const double span = gd.source_hi - gd.source_lo;
+                x0 = gd.source_lo + span * ((double)r.x * 2.3283064365386963e-10);
+                y0 = gd.source_lo + span * ((double)r.y * 2.3283064365386963e-10);
+                z0 = gd.source_lo + span * ((double)r.z * 2.3283064365386963e-10);
+            }
+            px = (float)x0; py = (float)y0; pz = (float)z0;
+            if (PERIODIC) {
+                if (px >= L) px = 0.f;
+                if (py >= L) py = 0.f;
+                if (pz >= L) pz = 0.f;
+            }
+            x0 = px; y0 = py; z0 = pz;
+        }
+        // ---- state ----
+        float dx = 0.f, dy = 0.f, dz = 0.f;           // unwrapped displacement from x0
+        float rx = 0.f, ry = 0.f, rz = 0.f, r2 = 0.f; // Tier-1 sphere centre (displacement) and radius^2
+        int cell = 0, inside = 0;
+        bool dead = !active;
+        bool frozen = !active;
+        uint32_t n_full = 0, n_t1 = 0, n_fb = 0, n_acc = 0, n_rej = 0, escaped = 0, cerr = 0;
+        if (active && cells) {
+            int s1 = 0, in = 0;
+            float rs = 0.f;
+            int st = classify_f32(g, px, py, pz, s1, in, rs);
+            if (st == CLS_FALLBACK) { st = classify_list_f64(g, px, py, pz, s1, in); rs = 0.f; ++n_fb; }
+            if (st != CLS_OK) { cerr = 1; dead = true; }
+            cell = cell_of(g, s1); inside = in; r2 = rs * rs; ++n_full;
+        }
+        double Yx = 0.0, Yy = 0.0, Yz = 0.0;          // Y' at the last storage point
+        float Sx = 0.f, Sy = 0.f, Sz = 0.f;           // sum of displacements in this interval
+        float ax = 0.f, ay = 0.f, az = 0.f;           // displacement at the interval start
+        float dM[MADI_MAX_PAIRS][3];
+#pragma unroll
+        for (int p = 0; p < MADI_MAX_PAIRS; ++p) { dM[p][0] = dM[p][1] = dM[p][2] = 0.f; }
+        const size_t row = (size_t)job.y_row + (size_t)local;
+        if (OUT == MADI_OUT_Y && active) {
+            d.Y[(row * d.n_grid) * 3 + 0] = 0.0;
+            d.Y[(row * d.n_grid) * 3 + 1] = 0.0;
+            d.Y[(row * d.n_grid) * 3 + 2] = 0.0;
+            d.inside_trace[row * d.n_grid] = (int8_t)inside;
+        }
+        {
+            const unsigned b = __ballot_sync(0xffffffffu, active && inside);
+            if (lane == 0 && b) atomicAdd(&occ[0], (unsigned)__popc(b));
+        }
+        const double half_L = 0.5 * gd.L;
+        const uint64_t thr1 = job.thr1, thr2 = job.thr2;
+        const bool always = job.pp >= 1.0;
+        float g3 = 0.f, g4 = 0.f, g5 = 0.f;
+        uint32_t acc_word_odd = 0;
+        int h_left = d.steps_per_h;
+        int jgrid = 0;
+        for (int step = 0; step < d.n_steps; ++step) {
+            // ---- random numbers ----
+            float nx, ny, nz;
+            uint32_t word = 0;
+            double ustream = 0.0;
+            if (stream) {
+                if (!dead) {
+                    const size_t o = ((size_t)step * job.n_walkers + local);
+                    nx = (float)d.incr[3 * o + 0];
+                    ny = (float)d.incr[3 * o + 1];
+                    nz = (float)d.incr[3 * o + 2];
+                    ustream = d.unif[o];
+                } else { nx = ny = nz = 0.f; }
+            } else if ((step & 1) == 0) {
+                const uint32_t pair = (uint32_t)step >> 1;
+                const U4 ra = philox10(U4{widx, pair, 0u, 0u}, job.key0, job.key1);
+                const U4 rb = philox10(U4{widx, pair, 1u, 0u}, job.key0, job.key1);
+                float g0, g1, g2;
+                box_muller(ra.x, ra.y, g0, g1);
+                box_muller(ra.z, ra.w, g2, g3);
+                box_muller(rb.x, rb.y, g4, g5);
+                nx = g0 * sigma; ny = g1 * sigma; nz = g2 * sigma;
+                word = rb.z;
+                acc_word_odd = rb.w;
+            } else {
+                nx = g3 * sigma; ny = g4 * sigma; nz = g5 * sigma;
+                word = acc_word_odd;
+            }
+            if (!dead) {
+                float qx = px + nx, qy = py + ny, qz = pz + nz;
+                bool ok = true;
+                if (PERIODIC) {
+                    if (qx < 0.f) qx += L;
+                    if (qx >= L) qx -= L;
+                    if (qy < 0.f) qy += L;
+                    if (qy >= L) qy -= L;
+                    if (qz < 0.f) qz += L;
+                    if (qz >= L) qz -= L;
+                } else if (qx < 0.f || qx >= L || qy < 0.f || qy >= L || qz < 0.f || qz >= L) {
+                    ok = false;
+                    escaped = 1;
+                    dead = true;
+                }
+                if (ok) {
+                    const float ex = dx + nx, ey = dy + ny, ez = dz + nz;
+                    int ncell = 0, nin = 0;
+                    bool refreshed = false;
+                    float nr2 = 0.f;
+                    if (cells) {
+                        const float tx = ex - rx, ty = ey - ry, tz = ez - rz;
+                        const float disp2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
+                        if (disp2 < r2) {
+                            ncell = cell; nin = inside; ++n_t1;
+                        } else {
+                            int s1 = 0, in = 0;
+                            float rs = 0.f;
+                            int st = classify_f32(g, qx, qy, qz, s1, in, rs);
+                            if (st == CLS_FALLBACK) {
+                                st = classify_list_f64(g, qx, qy, qz, s1, in);
+                                rs = 0.f;
+                                ++n_fb;
+                            }
+                            ++n_full;
+                            if (st != CLS_OK) { cerr = 1; dead = true; }
+                            ncell = cell_of(g, s1); nin = in; nr2 = rs * rs; refreshed = true;
+                        }
+                    }
+                    if (!dead) {
+                        int m = 0;
+                        if (inside != nin) m = 1;
+                        else if (inside && nin && cell != ncell) m = 2;
+                        bool accept = true;
+                        if (m > 0 && !always) {
+                            if (stream) {
+                                const double thr = m == 1 ? job.pp : job.pp * job.pp;
+                                accept = ustream < thr;
+                            } else {
+                                const uint64_t thr = m == 1 ? thr1 : thr2;
+                                const uint32_t th = (uint32_t)(thr >> 32);
+                                if (word != th) {
+                                    accept = word < th;
+                                } else {
+                                    const U4 rc = philox10(U4{widx, (uint32_t)step, 2u, 0u}, job.key0, job.key1);
+                                    accept = rc.x < (uint32_t)thr;
+                                }
+                            }
+                            if (accept) ++n_acc; else ++n_rej;
+                        }
+                        if (accept) {
+                            px = qx; py = qy; pz = qz;
+                            dx = ex; dy = ey; dz = ez;
+                            cell = ncell; inside = nin;
+                            if (refreshed) { rx = ex; ry = ey; rz = ez; r2 = nr2; }
+                        }
+                    }
+                }
+            }
+            if (!dead) {
+                Sx += dx; Sy += dy; Sz += dz;
+            } else if (!frozen) {
+                // Walker stopped (fatal escape or classifier failure): close its
+                // trapezoid at the last accepted step and add nothing after.
+                frozen = true;
+                Yx += d.ts * ((double)Sx + 0.5 * ((double)ax - (double)dx));
+                Yy += d.ts * ((double)Sy + 0.5 * ((double)ay - (double)dy));
+                Yz += d.ts * ((double)Sz + 0.5 * ((double)az - (double)dz));
+                Sx = Sy = Sz = 0.f;
+                ax = dx; ay = dy; az = dz;
+            }
+            if (--h_left == 0) {
+                h_left = d.steps_per_h;
+                ++jgrid;
+                const double ts = d.ts;
+                Yx += ts * ((double)Sx + 0.5 * ((double)ax - (double)dx));
+                Yy += ts * ((double)Sy + 0.5 * ((double)ay - (double)dy));
+                Yz += ts * ((double)Sz + 0.5 * ((double)az - (double)dz));
+                Sx = Sy = Sz = 0.f;
+                ax = dx; ay = dy; az = dz;
+                if (OUT == MADI_OUT_Y) {
+                    if (active) {
+                        const double t = (double)jgrid * d.steps_per_h * ts;
+                        double* yo = d.Y + (row * d.n_grid + jgrid) * 3;
+                        yo[0] = y_ref(Yx, x0, half_L, t);
+                        yo[1] = y_ref(Yy, y0, half_L, t);
+                        yo[2] = y_ref(Yz, z0, half_L, t);
+                        d.inside_trace[row * d.n_grid + jgrid] = (int8_t)inside;
+                    }
+                } else {
+                    const Snap sn = snap[jgrid];
+                    if (sn.any) {
+                        const float fx = (float)Yx, fy = (float)Yy, fz = (float)Yz;
+#pragma unroll
+                        for (int p = 0; p < MADI_MAX_PAIRS; ++p) {
+                            const float k = snap_coef(sn.code, p);
+                            if (k != 0.f) {
+                                dM[p][0] = fmaf(k, fx, dM[p][0]);
+                                dM[p][1] = fmaf(k, fy, dM[p][1]);
+                                dM[p][2] = fmaf(k, fz, dM[p][2]);
+                            }
+                        }
+                    }
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, active && inside);
+                if (lane == 0 && b) atomicAdd(&occ[jgrid], (unsigned)__popc(b));
+            }
+        }
+        // ---- phase epilogue: per (pair, dir, b) warp sums -> fixed point ----
+        if (OUT == MADI_OUT_FUSED) {
+            const bool live = active && !escaped && !cerr;
+            for (int p = 0; p < d.n_pairs; ++p) {
+                float mx = 0.f, my = 0.f, mz = 0.f;
+#pragma unroll
+                for (int q = 0; q < MADI_MAX_PAIRS; ++q)
+                    if (q == p) { mx = dM[q][0]; my = dM[q][1]; mz = dM[q][2]; }
+                for (int u = 0; u < d.n_dirs; ++u) {
+                    const float proj = fmaf(d.dirs[3 * u], mx, fmaf(d.dirs[3 * u + 1], my, d.dirs[3 * u + 2] * mz));
+                    for (int bb = 0; bb < d.n_b; ++bb) {
+                        float c = 0.f, s = 0.f;
+                        if (live) sincosf(d.coef[p * d.n_b + bb] * proj, &s, &c);
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) {
+                            c += __shfl_xor_sync(0xffffffffu, c, o);
+                            s += __shfl_xor_sync(0xffffffffu, s, o);
+                        }
+                        if (lane == 0) {
+                            const int idx = ((p * d.n_b + bb) * d.n_dirs + u) * 2;
+                            atomicAdd(reinterpret_cast<unsigned long long*>(&acc[idx]),
+                                      (unsigned long long)__float2ll_rn(c * 4294967296.0f));
+                            atomicAdd(reinterpret_cast<unsigned long long*>(&acc[idx + 1]),
+                                      (unsigned long long)__float2ll_rn(s * 4294967296.0f));
+                        }
+                    }
+                }
+            }
+        }
+        // ---- counters ----
+        {
+            uint32_t v[8] = {active ? 1u : 0u, escaped, cerr, n_full, n_t1, n_fb, n_acc, n_rej};
+            uint64_t* cnt = d.counters + (size_t)job.slot * MADI_CNT_N;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const uint32_t s = __reduce_add_sync(0xffffffffu, v[i]);
+                if (lane == 0 && s) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[i]), (unsigned long long)s);
+            }
+        }
+        __syncthreads();
+        if (OUT == MADI_OUT_FUSED) {
+            long long* out = reinterpret_cast<long long*>(d.accum) + (size_t)job.slot * 2 * n_out;
+            for (int i = tid; i < 2 * n_out; i += nthr)
+                if (acc[i]) atomicAdd(reinterpret_cast<unsigned long long*>(&out[i]), (unsigned long long)acc[i]);
+        }
+        uint64_t* occ_out = d.occupancy + (size_t)job.slot * d.n_grid;
+        for (int j = tid; j < d.n_grid; j += nthr)
+            if (occ[j]) atomicAdd(reinterpret_cast<unsigned long long*>(&occ_out[j]), (unsigned long long)occ[j]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fp64 replay of a fixed random stream (golden check; madi/walker_gpu.py:698-840
+// arithmetic: separately rounded fp64, reference origin L/2, exact KD rule).
+// One thread per walker of jobs[0].
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) walk_f64_kernel(const madi_walk_desc d) {
+    const madi_walk_job job = d.jobs[0];
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= job.n_walkers) return;
+    const madi_geometry gd = d.geoms[job.geom];
+    const Geo g = make_geo(gd, reinterpret_cast<const unsigned char*>(gd.stage));
+    const bool periodic = gd.boundary == MADI_BOUNDARY_PERIODIC;
+    const bool cells = gd.has_cells != 0;
+    const double L = gd.L, half_L = gd.L / 2.0, ts = d.ts, pp = job.pp;
+    const size_t row = (size_t)job.y_row + w;
+    double px = d.init[3 * (size_t)w], py = d.init[3 * (size_t)w + 1], pz = d.init[3 * (size_t)w + 2];
+    int cell = 0, inside = 0, escaped = 0, cerr = 0;
+    uint32_t n_acc = 0, n_rej = 0, n_full = 0;
+    if (cells) {
+        int s1 = 0;
+        if (classify_kd_f64(g, px, py, pz, s1, inside) != CLS_OK) cerr = 1;
+        cell = __float_as_int(g.lo[s1].w);
+        ++n_full;
+    }
+    int kx = 0, ky = 0, kz = 0;
+    double xp = __dsub_rn(px, half_L), yp = __dsub_rn(py, half_L), zp = __dsub_rn(pz, half_L);
+    double Yx = 0.0, Yy = 0.0, Yz = 0.0;
+    double* Yo = d.Y + row * d.n_grid * 3;
+    int8_t* It = d.inside_trace + row * d.n_grid;
+    Yo[0] = Yo[1] = Yo[2] = 0.0;
+    It[0] = (int8_t)inside;
+    for (int step = 0; step < d.n_steps; ++step) {
+        if (!escaped && !cerr) {
+            const size_t o = (size_t)step * job.n_walkers + w;
+            double qx = __dadd_rn(px, d.incr[3 * o]), qy = __dadd_rn(py, d.incr[3 * o + 1]),
+                   qz = __dadd_rn(pz, d.incr[3 * o + 2]);
+            const double u = d.unif[o];
+            int qkx = kx, qky = ky, qkz = kz;
+            bool ok = true;
+            if (periodic) {
+                if (qx < 0.0) { qx = __dadd_rn(qx, L); --qkx; }
+                if (qx >= L) { qx = __dsub_rn(qx, L); ++qkx; }
+                if (qy < 0.0) { qy = __dadd_rn(qy, L); --qky; }
+                if (qy >= L) { qy = __dsub_rn(qy, L); ++qky; }
+                if (qz < 0.0) { qz = __dadd_rn(qz, L); --qkz; }
+                if (qz >= L) { qz = __dsub_rn(qz, L); ++qkz; }
+            } else if (qx < 0.0 || qx >= L || qy < 0.0 || qy >= L || qz < 0.0 || qz >= L) {
+                escaped = 1;
+                ok = false;
+            }
+            if (ok) {
+                int ncell = 0, nin = 0;
+                if (cells) {
+                    int s1 = 0;
+                    if (classify_kd_f64(g, qx, qy, qz, s1, nin) != CLS_OK) { cerr = 1; }
+                    ncell = __float_as_int(g.lo[s1].w);
+                    ++n_full;
+                }
+                if (!cerr) {
+                    int m = 0;
+                    if (inside && !nin) m = 1;
+                    else if (!inside && nin) m = 1;
+                    else if (inside && nin && cell != ncell) m = 2;
+                    bool accept = true;
+                    if (m > 0 && pp < 1.0) {
+                        const double thr = m == 1 ? pp : __dmul_rn(pp, pp);
+                        accept = !(u >= thr);
+                        if (accept) ++n_acc; else ++n_rej;
+                    }
+                    if (accept) {
+                        px = qx; py = qy; pz = qz; kx = qkx; ky = qky; kz = qkz;
+                        cell = ncell; inside = nin;
+                    }
+                    double xn = __dsub_rn(px, half_L), yn = __dsub_rn(py, half_L), zn = __dsub_rn(pz, half_L);
+                    if (periodic) {
+                        xn = __dadd_rn(xn, __dmul_rn((double)kx, L));
+                        yn = __dadd_rn(yn, __dmul_rn((double)ky, L));
+                        zn = __dadd_rn(zn, __dmul_rn((double)kz, L));
+                    }
+                    Yx = __dadd_rn(Yx, __dmul_rn(__dmul_rn(0.5, __dadd_rn(xp, xn)), ts));
+                    Yy = __dadd_rn(Yy, __dmul_rn(__dmul_rn(0.5, __dadd_rn(yp, yn)), ts));
+                    Yz = __dadd_rn(Yz, __dmul_rn(__dmul_rn(0.5, __dadd_rn(zp, zn)), ts));
+                    xp = xn; yp = yn; zp = zn;
+                }
+            }
+        }
+        const int si = step + 1;
+        if (si % d.steps_per_h == 0) {
+            const int j = si / d.steps_per_h;
+            Yo[3 * j] = Yx; Yo[3 * j + 1] = Yy; Yo[3 * j + 2] = Yz;
+            It[j] = (int8_t)inside;
+            if (inside) atomicAdd(reinterpret_cast<unsigned long long*>(&d.occupancy[(size_t)job.slot * d.n_grid + j]), 1ull);
+        }
+    }
+    uint64_t* cnt = d.counters + (size_t)job.slot * MADI_CNT_N;
+    atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[MADI_CNT_WALKERS]), 1ull);
+    if (escaped) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[MADI_CNT_ESCAPED]), 1ull);
+    if (cerr) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[MADI_CNT_CLASSIFIER_ERROR]), 1ull);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[MADI_CNT_FULL]), (unsigned long long)n_full);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[MADI_CNT_CROSS_ACCEPT]), (unsigned long long)n_acc);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[MADI_CNT_CROSS_REJECT]), (unsigned long long)n_rej);
+    const int8_t i0 = It[0];
+    if (i0) atomicAdd(reinterpret_cast<unsigned long long*>(&d.occupancy[(size_t)job.slot * d.n_grid]), 1ull);
+}
+
+// ---------------------------------------------------------------------------
+// Column reduction from stored Y (madi/walker_gpu.py:658-695): one CTA per
+// column, fp64 partials, deterministic tree.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) reduce_Y_kernel(const double* __restrict__ Y, int64_t n_walkers, int n_grid,
+                                                        const int32_t* jd, const int32_t* jD, const int32_t* js,
+                                                        const double* coef, double* cos_sum, double* sin_sum) {
+    __shared__ double sc[256], ss[256];
+    const int col = blockIdx.x;
+    const int a = jd[col], b = jD[col], c = js[col];
+    const double pc = coef[col];
+    double lc = 0.0, ls = 0.0;
+    const int64_t total = n_walkers * 3;
+    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
+        const int64_t w = i / 3;
+        const int ax = (int)(i - 3 * w);
+        const double* y = Y + (size_t)w * n_grid * 3;
+        const double dm = y[3 * a + ax] + y[3 * b + ax] - y[3 * c + ax];
+        double s, cc;
+        sincos(pc * dm, &s, &cc);
+        lc += cc;
+        ls += s;
+    }
+    sc[threadIdx.x] = lc;
+    ss[threadIdx.x] = ls;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) {
+            sc[threadIdx.x] += sc[threadIdx.x + st];
+            ss[threadIdx.x] += ss[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { cos_sum[col] = sc[0]; sin_sum[col] = ss[0]; }
+}
+
+}  // namespace madi
+
+using namespace madi;
+
+extern "C" int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walkers, int32_t n_grid) {
+    (void)tile_walkers;
+    const int64_t acc = 2ll * MADI_MAX_PAIRS * MADI_MAX_B * MADI_MAX_DIRS * 8;
+    return (int64_t)((stage_bytes + 15) & ~15) + acc + 4ll * n_grid + 8ll * n_grid + 16;
+}
+
+static int64_t fused_smem(const madi_walk_desc* d) {
+    const int64_t n_out = (int64_t)d->n_pairs * d->n_b * d->n_dirs;
+    return (int64_t)d->stage_smem + 16ll * n_out + 4ll * d->n_grid + 8ll * d->n_grid + 16;
+}
+
+template <bool STAGED, int OUT, bool PER>
+static madi_status launch_f32(const madi_walk_desc* d, cudaStream_t s) {
+    auto k = walk_f32_kernel<STAGED, OUT, PER>;
+    const int64_t sm = fused_smem(d);
+    if (sm > 227 * 1024) return host::fail(MADI_ERR_CAPACITY, "walker shared memory %lld B exceeds 227 KB", (long long)sm);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return host::cuda_fail(e, "cudaFuncSetAttribute(walker)");
+    const int blocks = d->grid_blocks > 0 ? d->grid_blocks : d->n_tiles;
+    k<<<blocks, d->tile_walkers, (size_t)sm, s>>>(*d);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return host::cuda_fail(e, "walker launch");
+    return MADI_OK;
+}
+
+extern "C" madi_status madi_walk(const madi_walk_desc* d, void* stream) {
+    host::clear_error();
+    if (!d) return host::fail(MADI_ERR_INVALID, "null walk descriptor");
+    if (d->n_jobs <= 0 || d->n_geoms <= 0 || !d->jobs || !d->geoms)
+        return host::fail(MADI_ERR_INVALID, "walk needs at least one job and one geometry");
+    if (d->n_steps < 0 || d->steps_per_h <= 0 || d->n_grid <= 0 || d->n_grid > MADI_MAX_GRID)
+        return host::fail(MADI_ERR_INVALID, "bad step grid (n_steps=%d steps_per_h=%d n_grid=%d)",
+                          d->n_steps, d->steps_per_h, d->n_grid);
+    if (d->n_steps / d->steps_per_h + 1 > d->n_grid)
+        return host::fail(MADI_ERR_INVALID, "n_grid too small for n_steps / steps_per_h");
+    if (!d->counters || !d->occupancy) return host::fail(MADI_ERR_INVALID, "counters and occupancy are required");
+    if (d->rng == MADI_RNG_STREAM && (!d->init || !d->incr || !d->unif))
+        return host::fail(MADI_ERR_INVALID, "stream replay needs init / incr / unif");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (d->precision == 64) {
+        if (d->rng != MADI_RNG_STREAM) return host::fail(MADI_ERR_UNSUPPORTED, "fp64 walker replays streams only");
+        if (d->n_jobs != 1) return host::fail(MADI_ERR_UNSUPPORTED, "fp64 replay walks one job");
+        if (!d->Y || !d->inside_trace) return host::fail(MADI_ERR_INVALID, "fp64 replay writes Y and inside_trace");
+        // The job is read on the device; the host only needs its walker count, passed as n_tiles * 128 bound.
+        const int blocks = d->n_tiles;
+        walk_f64_kernel<<<blocks, 128, 0, s>>>(*d);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return host::cuda_fail(e, "fp64 walker launch");
+        return MADI_OK;
+    }
+    if (d->precision != 32) return host::fail(MADI_ERR_INVALID, "precision must be 32 or 64");
+    if (d->tile_walkers <= 0 || d->tile_walkers > 256 || (d->tile_walkers & 31))
+        return host::fail(MADI_ERR_INVALID, "tile_walkers must be a multiple of 32 in [32, 256]");
+    if (d->grid_blocks > 0 && !d->work_counter) return host::fail(MADI_ERR_INVALID, "persistent launch needs a zeroed work counter");
+    if (d->out_mode == MADI_OUT_FUSED) {
+        if (d->n_pairs < 1 || d->n_pairs > MADI_MAX_PAIRS || d->n_b < 1 || d->n_b > MADI_MAX_B ||
+            d->n_dirs < 1 || d->n_dirs > MADI_MAX_DIRS)
+            return host::fail(MADI_ERR_UNSUPPORTED, "fused epilogue holds <= %d pairs, <= %d b, <= %d dirs",
+                              MADI_MAX_PAIRS, MADI_MAX_B, MADI_MAX_DIRS);
+        if ((int64_t)d->n_pairs * d->n_b * d->n_dirs > 2048)
+            return host::fail(MADI_ERR_UNSUPPORTED, "fused epilogue holds <= 2048 (column, direction) outputs");
+        if (!d->accum) return host::fail(MADI_ERR_INVALID, "fused output needs accum");
+        for (int p = 0; p < d->n_pairs; ++p)
+            if (d->pair_jd[p] < 0 || d->pair_jD[p] < 0 || d->pair_js[p] < 0 || d->pair_jd[p] >= d->n_grid ||
+                d->pair_jD[p] >= d->n_grid || d->pair_js[p] >= d->n_grid)
+                return host::fail(MADI_ERR_INVALID, "pair grid index out of range");
+    } else if (d->out_mode == MADI_OUT_Y) {
+        if (!d->Y || !d->inside_trace) return host::fail(MADI_ERR_INVALID, "Y output needs Y and inside_trace");
+    } else {
+        return host::fail(MADI_ERR_INVALID, "unknown out_mode");
+    }
+    if (d->stage_smem < 0 || (d->stage_smem & 15)) return host::fail(MADI_ERR_INVALID, "stage_smem must be a multiple of 16");
+    const bool staged = d->stage_smem > 0;
+    const bool per = d->boundary == MADI_BOUNDARY_PERIODIC;
+    madi_status st;
+    if (d->out_mode == MADI_OUT_FUSED) {
+        if (staged) st = per ? launch_f32<true, MADI_OUT_FUSED, true>(d, s) : launch_f32<true, MADI_OUT_FUSED, false>(d, s);
+        else st = per ? launch_f32<false, MADI_OUT_FUSED, true>(d, s) : launch_f32<false, MADI_OUT_FUSED, false>(d, s);
+    } else {
+        if (staged) st = per ? launch_f32<true, MADI_OUT_Y, true>(d, s) : launch_f32<true, MADI_OUT_Y, false>(d, s);
+        else st = per ? launch_f32<false, MADI_OUT_Y, true>(d, s) : launch_f32<false, MADI_OUT_Y, false>(d, s);
+    }
+    return st;
+}
+
+extern "C" madi_status madi_reduce_Y(const double* Y, int64_t n_walkers, int32_t n_grid, const int32_t* jd,
+                                     const int32_t* jD, const int32_t* js, const double* coef, int32_t n_cols,
+                                     double* cos_sum, double* sin_sum, void* stream) {
+    host::clear_error();
+    if (!Y || !jd || !jD || !js || !coef || !cos_sum || !sin_sum || n_walkers < 0 || n_grid <= 0 || n_cols < 0)
+        return host::fail(MADI_ERR_INVALID, "bad reduce_Y arguments");
+    if (n_cols == 0) return MADI_OK;
+    reduce_Y_kernel<<<n_cols, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(Y, n_walkers, n_grid, jd, jD, js,
+                                                                               coef, cos_sum, sin_sum);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return host::cuda_fail(e, "reduce_Y launch");
+    return MADI_OK;
+}

@@ -1,0 +1,78 @@
+"""Library match on the GPU (madi/fitters_gpu.py:414-463 entry points).
+
+``map_match_gpu`` / ``map_match_fits0_gpu`` keep the reference signatures and
+return shapes; ``precision`` selects the exhaustive FP32 scan or the BF16
+tensor-core scan with top-k FP32 rescoring.  Inputs are numpy (host) or torch
+CUDA tensors; outputs are numpy.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+
+try:
+    import torch
+    HAS_CUDA = bool(torch.cuda.is_available())
+except Exception:  # pragma: no cover
+    torch = None
+    HAS_CUDA = False
+
+DEFAULT_TOPK = 32
+
+
+def _as_dev(x):
+    if torch.is_tensor(x):
+        return x.to(device="cuda", dtype=torch.float32).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).cuda()
+
+
+def match_device(measured, lib_mat, *, free_s0: bool = False, precision: str = "fp32", topk: int = DEFAULT_TOPK,
+                 scratch=None, stream=None):
+    """Run madi_match on device tensors; returns (best_idx, best_resid, best_s0) device tensors."""
+    if not HAS_CUDA:
+        raise RuntimeError("CUDA is unavailable: the library match runs on a CUDA device only")
+    M = _as_dev(measured)
+    Lm = _as_dev(lib_mat)
+    if M.ndim != 2 or Lm.ndim != 2 or M.shape[1] != Lm.shape[1]:
+        raise ValueError("measured (n_vox, F) and library (n_lib, F) must share F")
+    n_vox, F = M.shape
+    prec = {"fp32": N.MADI_MATCH_FP32, "bf16": N.MADI_MATCH_BF16}[precision]
+    idx = torch.empty(n_vox, dtype=torch.int32, device=M.device)
+    res = torch.empty(n_vox, dtype=torch.float32, device=M.device)
+    s0 = torch.empty(n_vox, dtype=torch.float32, device=M.device) if free_s0 else None
+    need = int(N.lib().madi_match_scratch_bytes(n_vox, Lm.shape[0], F, prec, int(topk)))
+    if need > 0 and (scratch is None or scratch.numel() < need):
+        scratch = torch.empty(need, dtype=torch.uint8, device=M.device)
+    d = N.MadiMatchDesc()
+    d.measured, d.lib, d.n_vox, d.n_lib, d.n_feat = N.ptr(M), N.ptr(Lm), n_vox, Lm.shape[0], F
+    d.mode = N.MADI_MATCH_FREE_S0 if free_s0 else N.MADI_MATCH_FIXED_S0
+    d.precision, d.topk = prec, int(topk)
+    d.best_idx, d.best_resid, d.best_s0 = N.ptr(idx), N.ptr(res), N.ptr(s0)
+    d.scratch, d.scratch_bytes = (N.ptr(scratch), int(scratch.numel())) if need > 0 else (0, 0)
+    s = stream if stream is not None else torch.cuda.current_stream(M.device)
+    st = N.lib().madi_match(C.byref(d), s.cuda_stream)
+    N.check(st, "madi_match")
+    return idx, res, s0
+
+
+def map_match_gpu(measured_batch, lib_mat, kios_arr, rhos_arr, Vs_arr, *, precision: str = "fp32",
+                  topk: int = DEFAULT_TOPK):
+    """Fixed-S0 MAP: (kio, rho, V, resid) of the best library entry per voxel."""
+    idx, res, _ = match_device(measured_batch, lib_mat, precision=precision, topk=topk)
+    b = idx.cpu().numpy().astype(np.int64)
+    return (np.asarray(kios_arr)[b], np.asarray(rhos_arr)[b], np.asarray(Vs_arr)[b],
+            res.cpu().numpy().astype(np.float64))
+
+
+def map_match_fits0_gpu(raw_signal, lib_mat, kios_arr, rhos_arr, Vs_arr, *, precision: str = "fp32",
+                        topk: int = DEFAULT_TOPK):
+    """Free-S0 MAP: (kio, rho, V, resid, s0) of the best library entry per voxel."""
+    idx, res, s0 = match_device(raw_signal, lib_mat, free_s0=True, precision=precision, topk=topk)
+    b = idx.cpu().numpy().astype(np.int64)
+    return (np.asarray(kios_arr)[b], np.asarray(rhos_arr)[b], np.asarray(Vs_arr)[b],
+            res.cpu().numpy().astype(np.float64), s0.cpu().numpy().astype(np.float64))

@@ -1,0 +1,270 @@
+/*
+ * madi_gb300.h -- C ABI of the GB300 (sm_103a) MADI Monte Carlo diffusion path.
+ *
+ * The reference (jadenfigger/Custom_MADI) is Python with Numba-CUDA kernels; it
+ * has no foreign-function boundary of its own.  Each entry point below replaces
+ * one of its device launches (cited per function) and is bound from Python by
+ * custom_madi_gb300/_native.py through ctypes.
+ *
+ * Conventions
+ *   - Plain C types only: device pointers, sizes, a cudaStream_t passed as void*.
+ *   - Every function returns a madi_status; no exception crosses the ABI.  On
+ *     failure madi_last_error_string() holds a one-line reason (thread-local).
+ *   - The library never allocates device memory: every buffer, including the
+ *     zero-initialised scratch words named in the descriptors, belongs to the
+ *     caller.  Launches are asynchronous on the given stream.
+ *   - Units: um, ms.  Geometry is a cubic walk box [0, L)^3.
+ */
+#ifndef MADI_GB300_H
+#define MADI_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MADI_ABI_VERSION 1
+
+typedef enum madi_status {
+    MADI_OK = 0,
+    MADI_ERR_INVALID = 1,      /* bad argument or descriptor (ValueError upstream)          */
+    MADI_ERR_CUDA = 2,         /* a CUDA runtime call failed                                */
+    MADI_ERR_CAPACITY = 3,     /* an output or scratch capacity is too small                */
+    MADI_ERR_TIMEOUT = 4,      /* a bounded device or host wait ran out                     */
+    MADI_ERR_UNSUPPORTED = 5,  /* configuration this build does not handle                 */
+    MADI_ERR_GEOMETRY = 6      /* geometry the classifier cannot prove (RuntimeError)       */
+} madi_status;
+
+/* ------------------------------------------------------------------------ */
+/* Geometry                                                                 */
+/* ------------------------------------------------------------------------ */
+
+enum { MADI_BOUNDARY_FATAL = 0, MADI_BOUNDARY_PERIODIC = 1 };
+
+/*
+ * One ensemble resident in device memory.  Built on the host by
+ * custom_madi_gb300.ensemble (seeds as in madi/ensemble.py:585-638 and :679,
+ * KD tree as in :525-563) and packed into two device buffers:
+ *
+ *   stage  -- 16-byte aligned block copied whole into shared memory by the
+ *             walker when stage_bytes fits; otherwise read in place.
+ *             [ seed_hi : float4 x n_seeds ]  x,y,z rounded to fp32, w = alpha (fp32)
+ *             [ seed_lo : float4 x n_seeds ]  x,y,z residuals (x - hi), w = cell id bits
+ *             [ grid_offset : uint32 x (G^3 + 1), padded to 16 bytes ]
+ *             [ grid_ids : uint16 (or uint32 when ids_u32) x grid_total, padded ]
+ *   seed_f64 -- double4 x n_seeds: x, y, z, alpha (the exact geometry).
+ *   kd_*     -- balanced KD tree over the seeds, node 0 the root, -1 = none.
+ *
+ * grid_ids of voxel v (voxel edge grid_h) list every seed that can be the
+ * nearest seed of, or bind a shifted facet for, any point of the voxel grown by
+ * grid_eps, plus every seed whose facet can come within safe_cap of the
+ * contracted cell boundary: a proven superset, so the fp32 and fp64 rules run
+ * on these lists return the labels of the all-seed rule.
+ */
+typedef struct madi_geometry {
+    const void*    stage;          /* device, 16-byte aligned                     */
+    const double*  seed_f64;       /* device, [n_seeds][4]                        */
+    const int32_t* kd_seed;        /* device, [n_seeds]                           */
+    const int32_t* kd_left;        /* device, [n_seeds]                           */
+    const int32_t* kd_right;       /* device, [n_seeds]                           */
+    const int32_t* kd_parent;      /* device, [n_seeds]                           */
+    const int8_t*  kd_axis;        /* device, [n_seeds]                           */
+    uint32_t off_seed_lo;          /* byte offsets inside stage                   */
+    uint32_t off_grid_offset;
+    uint32_t off_grid_ids;
+    uint32_t stage_bytes;          /* multiple of 16                              */
+    int32_t  n_seeds;              /* seeds in the arrays (tiled images included) */
+    int32_t  grid_n;               /* voxels per axis (G)                         */
+    int32_t  ids_u32;              /* 1 when grid_ids are uint32                  */
+    int32_t  boundary;             /* MADI_BOUNDARY_*                             */
+    int32_t  has_cells;            /* 0 = free water (no membranes)               */
+    int32_t  pad0;
+    double   L;                    /* walk box edge                               */
+    double   grid_h;               /* voxel edge (G * grid_h >= L)                */
+    double   safe_cap;             /* Tier-1 radius cap the lists were built for  */
+    double   source_lo;            /* walkers start uniform in [lo, hi)^3         */
+    double   source_hi;
+} madi_geometry;
+
+/* Replaces Ensemble.classify_cpu (madi/ensemble.py:213-256) and the device
+ * classifier _classify_full_facet (madi/walker_gpu.py:272-335).
+ * points: device [n][3], fp64 (points_f32 = 0) or fp32 (points_f32 = 1), in
+ * [0, L)^3 (periodic points are wrapped by the caller).
+ * method 0 = stackless KD traversal in fp64 (the reference rule);
+ * method 1 = voxel-grid classifier in fp32 with an fp64 guard-band fallback.
+ * cell_out: nearest seed id (periodic: cell id of the seed); inside_out: 0/1;
+ * path_out (optional): 0 fp32 decision, 1 fp64 fallback, 2 KD fp64. */
+madi_status madi_classify(const madi_geometry* geom, const void* points, int points_f32,
+                          int64_t n, int method, int32_t* cell_out, uint8_t* inside_out,
+                          uint8_t* path_out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Walker                                                                   */
+/* ------------------------------------------------------------------------ */
+
+#define MADI_MAX_PAIRS 8
+#define MADI_MAX_B 32
+#define MADI_MAX_DIRS 32
+#define MADI_MAX_GRID 512
+
+enum { MADI_RNG_PHILOX = 0, MADI_RNG_STREAM = 1 };
+enum { MADI_OUT_FUSED = 0, MADI_OUT_Y = 1 };
+
+/* One walk job: one ensemble at one membrane probability (one (e, kio) pair of
+ * madi/walker_gpu.py:1218-1232), n_walkers walkers. */
+typedef struct madi_walk_job {
+    int32_t  geom;            /* index into the geometry array                       */
+    int32_t  n_walkers;
+    uint32_t walker_base;     /* Philox counter of the first walker (CRN identity)   */
+    uint32_t key0, key1;      /* Philox key: walk seed (madi/walker_gpu.py:81-83)   */
+    int32_t  slot;            /* accumulator slot receiving this job's sums          */
+    int32_t  tile_begin;      /* first work tile of this job (prefix over jobs)      */
+    int32_t  y_row;           /* first output row in Y / inside_trace (OUT_Y)       */
+    double   pp;              /* membrane transmission probability, [0, 1]           */
+    uint64_t thr1;            /* floor(pp   * 2^64), accept iff U64 < thr           */
+    uint64_t thr2;            /* floor(pp^2 * 2^64)                                  */
+} madi_walk_job;
+
+/* Device counters per slot (uint64 each), zeroed by the caller. */
+enum {
+    MADI_CNT_WALKERS = 0, MADI_CNT_ESCAPED, MADI_CNT_CLASSIFIER_ERROR,
+    MADI_CNT_FULL, MADI_CNT_TIER1, MADI_CNT_FALLBACK64, MADI_CNT_CROSS_ACCEPT,
+    MADI_CNT_CROSS_REJECT, MADI_CNT_N
+};
+
+/*
+ * Replaces _walk_kernel + _reduce_kernel (madi/walker_gpu.py:520-695), their
+ * launch in _run_walk_one_ensemble / _walk_and_reduce_one_ensemble
+ * (:843-951, :989-1063), and the per-ensemble / per-kio loop of
+ * run_simulation_multi_kio_reduced (:1218-1232): every job is one work list of
+ * walker tiles consumed by one persistent launch.
+ *
+ * Fused output (out_mode FUSED): for job j, accum[slot][col][dir][2] holds
+ * round(2^32 * sum over walkers of cos / sin (coef[col] * u_dir . dM_pair)), an
+ * exact 64-bit fixed-point sum (order independent), with
+ * dM = Y(delta) + Y(Delta) - Y(Delta + delta) per axis; occupancy[slot][j_grid]
+ * counts inside walkers at each Y grid point; counters[slot][MADI_CNT_*].
+ *
+ * Y output (out_mode Y): Y[y_row + w][j][3] (fp64, reference origin L/2 as in
+ * madi/walker_gpu.py:562-564) and inside_trace[y_row + w][j] (int8).
+ *
+ * rng MADI_RNG_STREAM replays init[w][3], incr[step][w][3], unif[step][w]
+ * (WalkRandomStream, madi/walker_gpu.py:86-127), fp64 arrays.
+ */
+typedef struct madi_walk_desc {
+    const madi_geometry* geoms;    /* device array                                    */
+    const madi_walk_job* jobs;     /* device array                                    */
+    int32_t n_geoms, n_jobs;
+    int32_t n_tiles;               /* total tiles over all jobs                       */
+    int32_t tile_walkers;          /* walkers per tile (= threads per block)          */
+    int32_t grid_blocks;           /* persistent CTAs; 0 = one per tile               */
+    int32_t stage_smem;            /* max stage_bytes over geoms; 0 = read in place   */
+    int32_t boundary;              /* MADI_BOUNDARY_* shared by every geometry        */
+    int32_t precision;             /* 32 = fp32 production walker, 64 = fp64 replay   */
+    int32_t rng;                   /* MADI_RNG_*                                      */
+    int32_t out_mode;              /* MADI_OUT_*                                      */
+    int32_t n_steps, steps_per_h, n_grid;
+    double  sigma, ts;
+    /* fused epilogue */
+    int32_t n_pairs, n_b, n_dirs, pad1;
+    int32_t pair_jd[MADI_MAX_PAIRS], pair_jD[MADI_MAX_PAIRS], pair_js[MADI_MAX_PAIRS];
+    float   coef[MADI_MAX_PAIRS * MADI_MAX_B];   /* phase coefficient per (pair, b)  */
+    float   dirs[MADI_MAX_DIRS * 3];
+    /* outputs */
+    int64_t*  accum;               /* [n_slots][n_pairs*n_b][n_dirs][2]               */
+    uint64_t* occupancy;           /* [n_slots][n_grid]                               */
+    uint64_t* counters;            /* [n_slots][MADI_CNT_N]                           */
+    double*   Y;                   /* OUT_Y: [rows][n_grid][3]                        */
+    int8_t*   inside_trace;        /* OUT_Y: [rows][n_grid]                           */
+    /* replay stream (MADI_RNG_STREAM) */
+    const double* init;            /* [n_walkers][3]                                  */
+    const double* incr;            /* [n_steps][n_walkers][3]                         */
+    const double* unif;            /* [n_steps][n_walkers]                            */
+    /* scratch: one zeroed uint32 work counter */
+    uint32_t* work_counter;
+} madi_walk_desc;
+
+madi_status madi_walk(const madi_walk_desc* desc, void* stream);
+
+/* Shared-memory bytes the fp32 walker needs for a geometry of stage_bytes. */
+int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walkers, int32_t n_grid);
+
+/* Replaces _reduce_kernel (madi/walker_gpu.py:658-695) for grids too large for
+ * the fused epilogue: Y [n_walkers][n_grid][3] fp64 -> cos_sum / sin_sum
+ * [n_cols] fp64 over the 3 axes, columns (jd, jD, js, coef). */
+madi_status madi_reduce_Y(const double* Y, int64_t n_walkers, int32_t n_grid,
+                          const int32_t* jd, const int32_t* jD, const int32_t* js,
+                          const double* coef, int32_t n_cols,
+                          double* cos_sum, double* sin_sum, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Library match                                                            */
+/* ------------------------------------------------------------------------ */
+
+enum { MADI_MATCH_FIXED_S0 = 0, MADI_MATCH_FREE_S0 = 1 };
+enum { MADI_MATCH_FP32 = 0, MADI_MATCH_BF16 = 1 };
+
+/*
+ * Replaces _map_kernel_fixed / _map_kernel_free_s0 and their launches
+ * (madi/fitters_gpu.py:96-154, :414-463), i.e. the argmin of
+ * match_voxels_batch (madi/library.py:1444-1450) and
+ * match_voxels_batch_fits0 (:1495-1522).
+ *   fixed S0: best = argmin_j (|L_j|^2 - 2 m.L_j), resid = |m|^2 + that
+ *   free  S0: best = argmin_j over m.L_j > 0 of |m|^2 - (m.L_j)^2/|L_j|^2
+ * Ties pick the lowest library index.
+ * FP32: exhaustive fp32 scan on the CUDA cores.
+ * BF16: tcgen05 BF16 x BF16 -> FP32 (TMEM) scores, a per-voxel top-k (k <= 32)
+ *       candidate list, then an fp32 rescore of the k candidates.
+ * measured: device fp32 [n_vox][n_feat]; lib: device fp32 [n_lib][n_feat].
+ * scratch: device buffer of madi_match_scratch_bytes(...) bytes (contents need
+ * no initialisation).
+ */
+typedef struct madi_match_desc {
+    const float* measured;
+    const float* lib;
+    int64_t n_vox;
+    int32_t n_lib, n_feat;
+    int32_t mode;                  /* MADI_MATCH_FIXED_S0 / FREE_S0 */
+    int32_t precision;             /* MADI_MATCH_FP32 / BF16       */
+    int32_t topk;                  /* BF16 candidates rescored     */
+    int32_t pad0;
+    int32_t* best_idx;             /* [n_vox]                      */
+    float*   best_resid;           /* [n_vox]                      */
+    float*   best_s0;              /* [n_vox] (free S0) or NULL    */
+    void*    scratch;
+    int64_t  scratch_bytes;
+} madi_match_desc;
+
+int64_t madi_match_scratch_bytes(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t precision,
+                                 int32_t topk);
+madi_status madi_match(const madi_match_desc* desc, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Host-side geometry builders (native C++; no device work)                 */
+/* ------------------------------------------------------------------------ */
+
+/* Balanced KD tree as in _build_gpu_kdtree (madi/ensemble.py:525-563): median
+ * on the widest-spread axis, preorder node numbering, root = node 0. */
+madi_status madi_kdtree_build(const double* seeds_xyz, int32_t n, int32_t* node_seed,
+                              int8_t* node_axis, int32_t* node_left, int32_t* node_right,
+                              int32_t* node_parent);
+
+/* Candidate lists of a G^3 voxel grid over [0, G*h)^3 (madi_geometry above).
+ * seeds: [n][4] x, y, z, alpha.  Two passes: call with ids == NULL to get
+ * *total, then with capacity >= *total. */
+madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h,
+                            double eps, double safe_cap, uint32_t* offsets,
+                            void* ids, int32_t ids_u32, int64_t capacity, int64_t* total);
+
+/* ------------------------------------------------------------------------ */
+/* Misc                                                                     */
+/* ------------------------------------------------------------------------ */
+int32_t madi_abi_version(void);
+const char* madi_last_error_string(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MADI_GB300_H */

@@ -1,0 +1,155 @@
+"""GPU walker parity: fixed-stream replays against the reference golden walk, and
+Philox walks against the oracle (same key: near-identical; independent key:
+within 3 Monte Carlo standard errors)."""
+
+import numpy as np
+import pytest
+
+from custom_madi_gb300.config import SimConfig
+
+pytestmark = pytest.mark.gpu
+
+C0 = dict(ts=0.01, T_max_ms=46.0, small_deltas=[6.0], big_deltas=[15.0, 25.0, 30.0, 40.0],
+          b_values=[0.0, 1000.0, 2500.0, 4000.0, 6000.0])
+
+
+def _golden_case(golden):
+    from custom_madi_gb300.ensemble import ensemble_from_arrays
+    from custom_madi_gb300.walker_gpu import WalkRandomStream
+    w = golden("golden_walk.npz")
+    ens = ensemble_from_arrays(w["seeds"], w["annulus"], float(w["L"]), source_lo=float(w["source_lo"]),
+                               source_hi=float(w["source_hi"]), rho_per_uL=1.0e6)
+    cfg = SimConfig(L=float(w["L"]), n_walkers=len(w["init"]), n_ensembles=1, ts=float(w["ts"]),
+                    T_max_ms=float(w["T_max_ms"]), h_ms=float(w["h_ms"]), small_deltas=[1.0, 2.0],
+                    big_deltas=[2.0, 3.0, 5.0], b_values=[0.0, 500.0, 1000.0, 2000.0])
+    stream = WalkRandomStream(w["init"], w["incr"], w["unif"])
+    return w, ens, cfg, stream
+
+
+def test_fp64_replay_matches_reference_golden(golden):
+    """Reference tolerance (scripts/run_gpu_golden_check.py:27-28): rtol 5e-11, atol 5e-12."""
+    from custom_madi_gb300.walker_gpu import run_walk_Y
+    w, ens, cfg, stream = _golden_case(golden)
+    Y, n_esc, tel = run_walk_Y(ens, 0.0, cfg, pp=float(w["pp"]), random_stream=stream, return_telemetry=True,
+                               verbose=False)
+    np.testing.assert_allclose(Y, w["Y"], rtol=5e-11, atol=5e-12)
+    assert np.array_equal(tel["inside_trace"], w["inside_trace"])
+    assert np.array_equal(tel["occupancy_fraction"], w["occupancy_fraction"])
+    assert n_esc == 0
+    print("fp64 replay max |dY| =", float(np.abs(Y - w["Y"]).max()))
+
+
+def test_fp32_replay_tracks_reference_golden(golden):
+    """Production fp32 walker on the same stream: labels identical, Y within fp32 rounding."""
+    from custom_madi_gb300.walker_gpu import run_walk_Y
+    w, ens, cfg, stream = _golden_case(golden)
+    Y, _, tel = run_walk_Y(ens, 0.0, cfg, pp=float(w["pp"]), random_stream=stream, return_telemetry=True,
+                           precision=32, verbose=False)
+    assert np.array_equal(tel["inside_trace"], w["inside_trace"])
+    np.testing.assert_allclose(Y, w["Y"], rtol=1e-6, atol=2e-3)
+
+
+def _periodic_c0(n_walkers, seed=0, n_cells=64):
+    from custom_madi_gb300.ensemble import create_ensemble
+    cfg = SimConfig(boundary_mode="periodic", n_cells=n_cells, n_walkers=n_walkers, n_ensembles=1,
+                    geometry_validation_points=50_000, geometry_vi_tolerance=0.05, **C0)
+    ens = create_ensemble(2.0e5, 4.0, cfg, seed=seed)
+    return cfg, ens
+
+
+def _oracle_sums(ens, cfg, cols, pp, key, n, dirs=None):
+    from oracle import oracle as O
+    from custom_madi_gb300.walker_gpu import pair_layout
+    lay = pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    out = O.walk(O.geom_arrays(ens), n_walkers=n, n_steps=cfg.n_steps, steps_per_h=cfg.steps_per_h,
+                 n_grid=cfg.n_grid, sigma=cfg.sigma, ts=cfg.ts, pp=pp, key=key, want_Y=False,
+                 columns=(lay.jd, lay.jD, lay.js, lay.coef), dirs=dirs)
+    cs = out["cos_sum"].reshape(lay.n_pairs * lay.n_b, -1)
+    return cs, out
+
+
+def test_philox_walk_same_key_tracks_oracle():
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.walker_gpu import WalkJob, simulate_jobs, kio_to_pp, PHILOX_KEY1
+    cfg, ens = _periodic_c0(2000)
+    cols = S.build_columns(cfg)
+    pp = kio_to_pp(20.0, ens.mean_AV, cfg)
+    res = simulate_jobs([WalkJob(ens, pp, 1234, 2000)], cfg, (cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef))
+    g = res[0]["cos"] / 2000.0
+    cs, out = _oracle_sums(ens, cfg, cols, pp, (1234, PHILOX_KEY1), 2000)
+    o = cs / 2000.0
+    assert np.max(np.abs(g - o)) < 5e-3
+    assert np.abs(res[0]["occupancy"] - out["occupancy"]).max() <= 0.02 * 2000
+    print("same-key max |dS| =", float(np.max(np.abs(g - o))), res[0]["counters"])
+
+
+def test_philox_walk_within_3_se_of_independent_oracle():
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.walker_gpu import WalkJob, simulate_jobs, kio_to_pp
+    cfg, ens = _periodic_c0(20000, seed=3)
+    cols = S.build_columns(cfg)
+    pp = kio_to_pp(20.0, ens.mean_AV, cfg)
+    ng, no = 20000, 3000
+    res = simulate_jobs([WalkJob(ens, pp, 99, ng)], cfg, (cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef))
+    Sg = res[0]["cos"].sum(axis=1) / (3.0 * ng)
+    cs, _ = _oracle_sums(ens, cfg, cols, pp, (777, 5), no)
+    So = cs.sum(axis=1) / (3.0 * no)
+    se = np.sqrt(np.maximum(1.0 - So ** 2, 1e-4) * (1.0 / ng + 1.0 / no))
+    assert np.all(np.abs(Sg - So) <= 3.0 * se + 1e-9), (Sg - So) / se
+
+
+def test_free_water_finite_lobe_matches_stejskal_tanner():
+    """tests/physics_audit/test_finite_delta_reference.py:35-61 criterion on the GPU walker."""
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.ensemble import create_dummy_ensemble
+    from custom_madi_gb300.walker_gpu import WalkJob, simulate_jobs
+    cfg = SimConfig(n_walkers=20000, n_ensembles=1, **C0)
+    ens = create_dummy_ensemble(cfg)
+    cols = S.build_columns(cfg)
+    r = simulate_jobs([WalkJob(ens, 0.0, 5, 20000)], cfg, (cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef))[0]
+    Sv = r["cos"].sum(axis=1) / (3 * 20000.0)
+    b = np.tile(np.asarray(cfg.b_values), 4)
+    expect = np.exp(-b * cfg.D0 * 1e-3)
+    se = np.sqrt(np.maximum(1 - Sv ** 2, 1e-6) / 20000.0)
+    assert np.all(np.abs(Sv - expect) <= 5 * se + 0.012)
+
+
+def test_fatal_escape_raises():
+    from custom_madi_gb300.ensemble import create_dummy_ensemble
+    from custom_madi_gb300.walker_gpu import WalkRandomStream, run_walk_Y
+    cfg = SimConfig(L=2.0, n_walkers=1, n_ensembles=1, T_max_ms=2.0, small_deltas=[1.0], big_deltas=[1.0],
+                    b_values=[0.0])
+    inc = np.zeros((cfg.n_steps, 1, 3))
+    inc[0, 0, 0] = 2.0
+    st = WalkRandomStream(np.array([[1.0, 1.0, 1.0]]), inc, np.zeros((cfg.n_steps, 1)))
+    for prec in (64, 32):
+        with pytest.raises(RuntimeError, match="fatal boundary condition"):
+            run_walk_Y(create_dummy_ensemble(cfg), 0.0, cfg, pp=0.0, random_stream=st, precision=prec, verbose=False)
+
+
+def test_trapezoid_known_answer(golden):
+    from custom_madi_gb300.ensemble import create_dummy_ensemble
+    from custom_madi_gb300.walker_gpu import WalkRandomStream, run_walk_Y
+    t = golden("trapezoid.npz")
+    cfg = SimConfig(L=200.0, n_walkers=1, n_ensembles=1, T_max_ms=2.0, h_ms=1.0, small_deltas=[1.0],
+                    big_deltas=[1.0, 2.0], b_values=[0.0, 1000.0])
+    st = WalkRandomStream(t["init"], t["incr"], t["unif"])
+    Y, _ = run_walk_Y(create_dummy_ensemble(cfg), 0.0, cfg, pp=0.0, random_stream=st, verbose=False)
+    assert np.array_equal(Y, t["Y"])
+
+
+def test_job_result_is_identical_alone_and_in_a_mixed_batch():
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.walker_gpu import WalkJob, simulate_jobs
+    cfg, ens = _periodic_c0(3000)
+    _, ens2 = _periodic_c0(3000, seed=9, n_cells=40)
+    cols = S.build_columns(cfg)
+    c = (cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    a = WalkJob(ens, 0.01, 42, 3000)
+    alone = simulate_jobs([a], cfg, c)[0]
+    again = simulate_jobs([a], cfg, c)[0]
+    mixed = simulate_jobs([WalkJob(ens2, 0.02, 7, 5000), a, WalkJob(ens, 0.0, 1, 700)], cfg, c)[1]
+    assert np.array_equal(alone["cos_fixed"], again["cos_fixed"])
+    assert np.array_equal(alone["cos_fixed"], mixed["cos_fixed"])
+    assert np.array_equal(alone["sin_fixed"], mixed["sin_fixed"])
+    assert np.array_equal(alone["occupancy"], mixed["occupancy"])

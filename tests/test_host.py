@@ -1,0 +1,180 @@
+"""Host-side logic and the C ABI boundary (no GPU work)."""
+
+import ctypes as C
+import json
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from custom_madi_gb300 import _native as N
+from custom_madi_gb300 import config as cfgmod
+from custom_madi_gb300 import ensemble as E
+from custom_madi_gb300.config import SimConfig
+from oracle import oracle as O
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+# ------------------------------------------------------------------ C ABI
+def test_library_exports_every_declared_symbol():
+    header = (ROOT / "include" / "madi_gb300.h").read_text()
+    declared = set(re.findall(r"^\s*(?:madi_status|int64_t|int32_t|const char\*)\s+(madi_\w+)\s*\(", header, re.M))
+    assert declared >= set(N.EXPORTED) - {"madi_last_error_string"}
+    lib = N.lib()
+    for name in sorted(declared | set(N.EXPORTED)):
+        assert hasattr(lib, name), name
+    assert lib.madi_abi_version() == 1
+
+
+def test_struct_layout_matches_header(tmp_path):
+    """ctypes mirrors == the C compiler's layout of the header structs."""
+    structs = {"madi_geometry": N.MadiGeometry, "madi_walk_job": N.MadiWalkJob,
+               "madi_walk_desc": N.MadiWalkDesc, "madi_match_desc": N.MadiMatchDesc}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/madi_gb300.h"', "int main(void){"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0;}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-o", str(exe), str(src)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n") if l)
+    for cname, py in structs.items():
+        assert int(got[cname]) == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
+
+
+def test_error_string_and_invalid_arguments():
+    lib = N.lib()
+    st = lib.madi_kdtree_build(None, 0, None, None, None, None, None)
+    assert st == N.MADI_ERR_INVALID
+    assert b"kdtree_build" in lib.madi_last_error_string()
+    with pytest.raises(ValueError, match="kdtree_build"):
+        N.check(st, "madi_kdtree_build")
+
+
+# ------------------------------------------------------------------ config
+def test_config_accepts_periodic_and_validates():
+    SimConfig(boundary_mode="periodic", small_deltas=[6.0], big_deltas=[15.0], T_max_ms=21.0).assert_grid_alignment()
+    with pytest.raises(ValueError, match="boundary_mode"):
+        SimConfig(boundary_mode="reflect", small_deltas=[1.0], big_deltas=[1.0], T_max_ms=2.0).assert_grid_alignment()
+    with pytest.raises(ValueError, match="integer multiple"):
+        cfgmod.grid_time_index(1.5, 1.0)
+    with pytest.raises(ValueError, match="T_max_ms"):
+        SimConfig(small_deltas=[30.0], big_deltas=[80.0], T_max_ms=100.0).assert_grid_alignment()
+    with pytest.raises(RuntimeError):
+        SimConfig().grid_size
+    c = SimConfig()
+    assert np.isclose(c.sigma, np.sqrt(2 * 3.0 * 1e-3)) and c.n_grid == 129 and c.steps_per_h == 1000
+    u = cfgmod.fibonacci_directions(24)
+    assert u.shape == (24, 3) and np.allclose(np.linalg.norm(u, axis=1), 1.0)
+    assert abs(np.mean(u, axis=0)).max() < 0.05
+
+
+def test_analytic_values_vs_reference(golden):
+    an = json.loads((ROOT / "tests" / "golden" / "analytic.json").read_text())
+    for vi, rho, a in an["alpha_star"]:
+        assert E.alpha_star_from_vi(vi, rho) == pytest.approx(a, rel=1e-12, abs=1e-15)
+    c0 = SimConfig(ts=0.01, T_max_ms=46.0, small_deltas=[6.0], big_deltas=[15.0, 25.0, 30.0, 40.0],
+                   b_values=[0.0, 1000.0, 2500.0, 4000.0, 6000.0])
+    for vi, rho, av in an["mean_AV"]:
+        assert E.governing_mean_A_over_V(vi, rho, c0)[0] == pytest.approx(av, rel=1e-14)
+    for rho, tm, side in an["si_domain_side"]:
+        assert E.si_domain_side_um(rho, SimConfig(T_max_ms=tm, small_deltas=[1.0], big_deltas=[1.0])) == pytest.approx(side, rel=1e-14)
+    from custom_madi_gb300 import walker_gpu as W
+    from custom_madi_gb300 import signal as S
+    for k, av, pp in an["kio_to_pp"]:
+        assert W.kio_to_pp(k, av, c0) == pytest.approx(pp, rel=1e-15)
+    for b, d, D, G in an["G_from_b"]:
+        assert S.G_from_b(b, d, D) == pytest.approx(G, rel=1e-15)
+    cols = S.build_columns(c0)
+    ref = an["c0_columns"]
+    for key in ("j_delta", "j_Delta", "j_sum"):
+        assert getattr(cols, key).tolist() == ref[key]
+    np.testing.assert_allclose(cols.phase_coef, ref["phase_coef"], rtol=1e-15)
+    assert len(cfgmod.valid_delta_pairs()) == an["default_pairs_count"]
+    for s, e, ws, es in an["walk_seed"]:
+        assert W._walk_seed(s, e) == ws and W._ensemble_seed(s, e) == es
+    with pytest.raises(ValueError, match=r"\[0, 1\]"):
+        W.kio_to_pp(1.0e7, 0.5, c0)
+
+
+def test_kdtree_builder_matches_reference_layout(golden):
+    k = golden("kdtree.npz")
+    seed, axis, left, right, parent = E._build_gpu_kdtree(k["seeds"])
+    assert np.array_equal(seed, k["node_seed"]) and np.array_equal(axis, k["node_axis"])
+    assert np.array_equal(left, k["node_left"]) and np.array_equal(right, k["node_right"])
+    assert np.array_equal(parent, k["node_parent"])
+
+
+def test_population_draw_order_matches_reference(golden):
+    p = golden("population.npz")
+    cfg = SimConfig(L=None, T_max_ms=float(p["T_max_ms"]), small_deltas=[1.0], big_deltas=[1.0])
+    side = E.si_domain_side_um(float(p["rho"]), cfg)
+    assert side == pytest.approx(float(p["L"]))
+    rng = np.random.default_rng(int(p["seed"]))
+    seeds, _, nn, cert = E._make_population(float(p["rho"]) * 1e-9, side, cfg, rng)
+    vi = float(p["rho"]) * float(p["V"]) * 1e-6
+    ann = np.minimum(E.alpha_star_from_vi(vi, float(p["rho"])), 0.9 * nn / 2.0)
+    assert np.array_equal(seeds, p["seeds"])
+    np.testing.assert_allclose(ann, p["annulus"], rtol=1e-14)
+    assert json.loads(str(p["certificate"]))["s10_pass"] == cert.s10_pass
+
+
+def _grid_superset_check(seeds, ann, L, G, h, cap, n_pts, rng):
+    xyza = np.column_stack([seeds, ann])
+    eps = 1e-4 * h + 1e-6 * L
+    off, ids, _ = E.build_voxel_grid(xyza, G, h, eps, cap)
+    pts = rng.uniform(0.0, L, size=(n_pts, 3))
+    amax = float(np.max(ann))
+    for p in pts:
+        v = np.minimum((p / h).astype(int), G - 1)
+        vox = (v[2] * G + v[1]) * G + v[0]
+        lst = set(ids[off[vox]:off[vox + 1]].tolist())
+        d = np.linalg.norm(seeds - p, axis=1)
+        need = set(np.flatnonzero(d <= d.min() + 2 * amax + 2 * cap).tolist())
+        assert need <= lst
+    return off, ids
+
+
+def test_voxel_grid_lists_are_proven_supersets(golden):
+    d = golden("classify_si.npz")
+    L = float(d["L"])
+    G, h, cap = E.default_grid_params(5.0e5, float(np.max(d["annulus"])), L)
+    off, ids = _grid_superset_check(d["seeds"], d["annulus"], L, G, h, cap, 3000, np.random.default_rng(1))
+    assert len(off) == G ** 3 + 1 and off[-1] == len(ids)
+
+
+def test_periodic_tiling_is_classification_equivalent(golden):
+    """The margin-limited image set labels points exactly like the full 27-image tiling."""
+    d = golden("classify_periodic.npz")
+    ens = E.ensemble_from_arrays(d["base_seeds"], d["annulus"], float(d["L"]), source_lo=0.0,
+                                 source_hi=float(d["L"]), rho_per_uL=float(d["rho"]), boundary_mode="periodic")
+    g = O.geom_arrays(ens)
+    c, i = O.classify_brute(g, d["points"])
+    assert np.array_equal(i, d["inside"]) and np.array_equal(c, d["cell"])
+    assert len(ens.classifier_seeds) < 27 * 64
+
+
+def test_pair_layout_and_thresholds():
+    from custom_madi_gb300 import walker_gpu as W
+    from custom_madi_gb300 import signal as S
+    c0 = SimConfig(ts=0.01, T_max_ms=46.0, small_deltas=[6.0], big_deltas=[15.0, 25.0, 30.0, 40.0],
+                   b_values=[0.0, 1000.0, 2500.0, 4000.0, 6000.0])
+    cols = S.build_columns(c0)
+    lay = W.pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    assert lay.n_pairs == 4 and lay.n_b == 5
+    assert lay.col_of.ravel().tolist() == list(range(20))
+    assert W.fused_supported(lay, 24) and not W.fused_supported(lay, 33)
+    t1, t2 = W._thresholds(0.25)
+    assert t1 == 1 << 62 and t2 == 1 << 60
+    assert W._thresholds(1.0)[0] == (1 << 64) - 1
+    m = W._membrane_transition_counts([1, 1, 1, 1, 1], [True, False, True, True, False], [1, 1, 2, 1, 1],
+                                      [False, True, True, True, False])
+    assert m.tolist() == [1, 1, 2, 0, 0]
