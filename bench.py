@@ -1,0 +1,354 @@
+"""Benchmark: batched library-build walker (the path's headline metric).
+
+Workload (one "step"): 256 library entries, each a periodic box of 27-512
+contracted Voronoi cells with (kio, rho, V) drawn log-uniform (kio 1-130 1/s,
+rho 4.4e3-5.8e7 cells/uL, V 0.01-206 pL, 0.5 <= v_i <= 0.99), 1e5 fp32 walkers
+per entry, dt = 0.01 ms, 4,600 steps, PGSE delta = 6 ms, Delta = 15/25/30/40 ms,
+5 b values, 24 gradient directions; all entries in one persistent launch.
+Metric: walker-steps/s over the whole job (all ranks).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Under torchrun each rank walks its own 256 entries (weak scaling, no
+collective on the data path); rank 0 prints one JSON line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "walker-steps/s"
+CONFIG_NAME = "batched library build: 256 entries x 1e5 walkers x 4600 steps, 27-512 cells, 20 cols x 24 dirs"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_walk_rate(ensembles, jobs, cfg, dirs, budget_s: float, threads: int, step_label: str = ""):
+    """Oracle (C restatement) walker-steps/s on a bounded sample of the same entries."""
+    from oracle import oracle as O
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.walker_gpu import PHILOX_KEY1, pair_layout
+    cols = S.build_columns(cfg)
+    lay = pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    # calibrate on a small sample
+    n0 = max(threads * 4, 64)
+    t0 = time.perf_counter()
+    O.walk(O.geom_arrays(jobs[0].ensemble), n_walkers=n0, n_steps=cfg.n_steps, steps_per_h=cfg.steps_per_h,
+           n_grid=cfg.n_grid, sigma=cfg.sigma, ts=cfg.ts, pp=jobs[0].pp, key=(jobs[0].walk_seed, PHILOX_KEY1),
+           want_Y=False, columns=(lay.jd, lay.jD, lay.js, lay.coef), dirs=dirs, n_threads=threads)
+    rate0 = n0 * cfg.n_steps / (time.perf_counter() - t0)
+    n_entries = min(8, len(jobs))
+    per = max(threads, int(rate0 * budget_s / (cfg.n_steps * n_entries)))
+    steps = 0
+    t0 = time.perf_counter()
+    for j in jobs[:n_entries]:
+        O.walk(O.geom_arrays(j.ensemble), n_walkers=per, n_steps=cfg.n_steps, steps_per_h=cfg.steps_per_h,
+               n_grid=cfg.n_grid, sigma=cfg.sigma, ts=cfg.ts, pp=j.pp, key=(j.walk_seed, PHILOX_KEY1),
+               want_Y=False, columns=(lay.jd, lay.jD, lay.js, lay.coef), dirs=dirs, n_threads=threads)
+        steps += per * cfg.n_steps
+    dt = time.perf_counter() - t0
+    return steps / dt, f"{n_entries} of the entries x {per} walkers x {cfg.n_steps} steps ({dt:.1f} s)"
+
+
+def build_workload(rank: int, n_entries: int, n_walkers: int, threads: int):
+    from custom_madi_gb300 import workloads as WL
+    from custom_madi_gb300.walker_gpu import WalkJob, kio_to_pp, _walk_seed
+    cfg = WL.batch_config(n_walkers=n_walkers)
+    trip = WL.batch_triplets(n_entries, seed=1 + 1000 * rank)
+    t0 = time.perf_counter()
+    ens = WL.build_ensembles(trip, cfg, seed=1000 * rank, threads=threads)
+    t_build = time.perf_counter() - t0
+    jobs = [WalkJob(e, kio_to_pp(t[0], e.mean_AV, cfg), _walk_seed(0, 0), n_walkers) for e, t in zip(ens, trip)]
+    return cfg, ens, jobs, t_build
+
+
+def run_reference_arm(args, ws, rank):
+    if rank != 0:
+        return 0
+    threads = len(os.sched_getaffinity(0))
+    cfg, ens, jobs, _ = build_workload(0, 16, args.walkers, threads)
+    dirs = cfg.direction_array()
+    rates = []
+    for i in range(args.warmup + args.steps):
+        r, sample = cpu_walk_rate(ens, jobs, cfg, dirs, budget_s=args.ref_budget, threads=threads)
+        if i >= args.warmup:
+            rates.append(r)
+    v = float(np.mean(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "walker-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": CONFIG_NAME, "arm": "oracle CPU restatement of _walk_cpu (madi/walker_gpu.py:698-840)"},
+            "cpu_baseline": {"value": v, "unit": "walker-steps/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--entries", type=int, default=256)
+    ap.add_argument("--walkers", type=int, default=100_000)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--ref-budget", type=float, default=8.0)
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shape (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    args = ap.parse_args(argv)
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        return run_reference_arm(args, ws, rank)
+
+    import torch
+    import torch.distributed as dist
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.walker_gpu import LaunchConfig, WalkBatch, pair_layout
+    from custom_madi_gb300 import autotune
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=dev) if "device_id" in dist.init_process_group.__code__.co_varnames \
+            else dist.init_process_group("nccl")
+    threads = len(os.sched_getaffinity(0))
+    cfg, ens, jobs, t_build = build_workload(rank, args.entries, args.walkers, threads)
+    cols = S.build_columns(cfg)
+    lay = pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    dirs = cfg.direction_array()
+    launch = LaunchConfig() if args.no_autotune else autotune.choose(jobs, cfg, lay, dirs, device=dev)
+    batch = WalkBatch(jobs, cfg, layout=lay, dirs=dirs, launch=launch, device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > 129 MB L2
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        batch.launch()
+    torch.cuda.synchronize(dev)
+    counters = batch.counters_np().sum(axis=0)
+    # ---- timed region (device-resident inputs) ----
+    peaks, peak_kind = _peaks()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    ev = []
+    with ClockSampler(local) as clk:
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            batch.launch()
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize(dev)
+        t_wall = time.perf_counter() - t_wall0
+    if ws > 1:
+        dist.barrier()
+    dev_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    steps_per_run = sum(j.n_walkers for j in jobs) * cfg.n_steps
+    t_max = dev_s
+    if ws > 1:
+        t = torch.tensor([dev_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = ws * steps_per_run * args.steps / t_max
+    # ---- end to end: host geometry + job tables -> device -> walk -> host sums ----
+    host = batch.host_mirror()
+    e2e_t = []
+    for i in range(0 if args.no_e2e else args.steps + 1):
+        t0 = time.perf_counter()
+        out = batch.run_from_host(host)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_t[1:])) if len(e2e_t) > 1 else float("nan")
+    e2e_val = steps_per_run / e2e_s * ws
+    # ---- roofline (issue bound: lane-operations per walker-step) ----
+    n_ws = max(int(counters[0]) * cfg.n_steps, 1)
+    f_full = counters[3] / n_ws
+    f_t1 = counters[4] / n_ws
+    k_mean = float(np.average([g.candidates_mean for g in batch.geoms]))
+    ops_step = 255.0 + f_full * 25.0 * k_mean + f_t1 * 12.0
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak_ops = sm_count * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    achieved = (steps_per_run * args.steps / dev_s) * ops_step / 1e12
+    traffic = None
+    tp = ROOT / "profiles" / "walk_f32_traffic.json"
+    if tp.exists():
+        per_ws = json.loads(tp.read_text()).get("dram_bytes_per_walker_step")
+        if per_ws is not None:
+            traffic = float(per_ws) * steps_per_run
+    line = {
+        "metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_s / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": CONFIG_NAME, "entries_per_gpu": len(jobs), "walkers_per_entry": args.walkers,
+                   "n_steps": cfg.n_steps, "columns": 20, "directions": len(dirs), "l2": "flushed (256 MB write) between steps",
+                   "tile_walkers": batch.desc.tile_walkers, "grid_blocks": batch.desc.grid_blocks,
+                   "staged_smem_bytes": int(batch.desc.stage_smem), "parallelism": f"replicas{ws}"},
+        "roofline": {"bound": "issue", "achieved": achieved, "peak": peak_ops, "unit": "Top/s",
+                     "frac": achieved / peak_ops, "traffic": traffic,
+                     "note": f"lane-ops per walker-step {ops_step:.1f} (255 RNG+move, 25 x {k_mean:.1f} candidates "
+                             f"x {f_full:.3f} full classifications, 12 x {f_t1:.3f} Tier-1); peak = SMs x 128 lanes x "
+                             f"sm_max_mhz ({peak_kind} clock)"},
+        "e2e": {"value": e2e_val, "unit": "walker-steps/s", "h2d_bytes_per_step": int(host["h2d_bytes"]),
+                "d2h_bytes_per_step": int(host["d2h_bytes"])},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "staged_fraction": batch.staged_fraction,
+        "walker_counters": {"full_per_step": float(f_full), "tier1_per_step": float(f_t1),
+                            "fallback64": int(counters[5]), "escaped": int(counters[1]),
+                            "classifier_error": int(counters[2])},
+        "host_ensemble_build_s": t_build,
+        "wall_s_timed": t_wall,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        r, sample = cpu_walk_rate(ens, jobs, cfg, dirs, budget_s=args.cpu_budget, threads=threads)
+        line["cpu_baseline"] = {"value": r, "unit": "walker-steps/s", "cores": threads, "kind": "port",
+                                "sample": sample}
+    if rank == 0 and ws == 1 and not args.no_secondary:
+        line["secondary"] = secondary(dev)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def secondary(dev):
+    """Plain one-entry-per-launch walker and the library match (BF16 vs FP32)."""
+    import torch
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300 import workloads as WL
+    from custom_madi_gb300.ensemble import create_ensemble
+    from custom_madi_gb300.fitters_gpu import match_device
+    from custom_madi_gb300.walker_gpu import LaunchConfig, WalkBatch, WalkJob, kio_to_pp, pair_layout
+    out = {}
+    cfg = WL.plain_config()
+    ens = create_ensemble(2.0e5, 4.0, cfg, seed=0)
+    cols = S.build_columns(cfg)
+    lay = pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    b = WalkBatch([WalkJob(ens, kio_to_pp(20.0, ens.mean_AV, cfg), 0, cfg.n_walkers)], cfg, layout=lay,
+                  dirs=cfg.direction_array(), launch=LaunchConfig(tile_walkers=128, persistent=False), device=dev)
+    for _ in range(3):
+        b.launch()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        b.launch()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    t = e0.elapsed_time(e1) / 5e3
+    out["plain_c0_walker_steps_per_s"] = cfg.n_walkers * cfg.n_steps / t
+    out["plain_c0_ms"] = t * 1e3
+    lib, _ = WL.match_library()
+    vox, truth = WL.rician_voxels(lib)
+    L = torch.from_numpy(lib.astype(np.float32)).to(dev)
+    M = torch.from_numpy(vox.astype(np.float32)).to(dev)
+    for prec in ("fp32", "bf16"):
+        try:
+            match_device(M[:4096], L, precision=prec)
+            torch.cuda.synchronize(dev)
+            e0.record()
+            idx, _, _ = match_device(M, L, precision=prec)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            t = e0.elapsed_time(e1) / 1e3
+            out[f"match_{prec}_voxels_per_s"] = len(vox) / t
+            out[f"match_{prec}_ms"] = t * 1e3
+            out[f"match_{prec}_idx"] = idx
+        except Exception as exc:  # report, do not hide
+            out[f"match_{prec}_error"] = str(exc)[:200]
+    if "match_fp32_idx" in out and "match_bf16_idx" in out:
+        out["match_bf16_fp32_index_agreement"] = float((out["match_fp32_idx"] == out["match_bf16_idx"]).float().mean())
+    out.pop("match_fp32_idx", None)
+    out.pop("match_bf16_idx", None)
+    return out
+
+
+if __name__ == "__main__":
+    sys.exit(main())

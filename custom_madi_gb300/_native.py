@@ -43,7 +43,7 @@ MADI_CNT_N = len(CNT_NAMES)
 EXPORTED = (
     "madi_abi_version", "madi_last_error_string", "madi_classify", "madi_walk",
     "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_scratch_bytes",
-    "madi_kdtree_build", "madi_grid_build",
+    "madi_kdtree_build", "madi_grid_build", "madi_walk_blocks_per_sm",
 )
 
 
@@ -52,12 +52,12 @@ class MadiGeometry(C.Structure):
         ("stage", C.c_void_p), ("seed_f64", C.c_void_p), ("kd_seed", C.c_void_p),
         ("kd_left", C.c_void_p), ("kd_right", C.c_void_p), ("kd_parent", C.c_void_p),
         ("kd_axis", C.c_void_p),
-        ("off_seed_lo", C.c_uint32), ("off_grid_offset", C.c_uint32),
+        ("off_cell", C.c_uint32), ("off_grid_offset", C.c_uint32),
         ("off_grid_ids", C.c_uint32), ("stage_bytes", C.c_uint32),
         ("n_seeds", C.c_int32), ("grid_n", C.c_int32), ("ids_u32", C.c_int32),
         ("boundary", C.c_int32), ("has_cells", C.c_int32), ("pad0", C.c_int32),
         ("L", C.c_double), ("grid_h", C.c_double), ("safe_cap", C.c_double),
-        ("source_lo", C.c_double), ("source_hi", C.c_double),
+        ("source_lo", C.c_double), ("source_hi", C.c_double), ("coord_err", C.c_double),
     ]
 
 
@@ -79,7 +79,7 @@ class MadiWalkDesc(C.Structure):
         ("out_mode", C.c_int32), ("n_steps", C.c_int32), ("steps_per_h", C.c_int32),
         ("n_grid", C.c_int32),
         ("sigma", C.c_double), ("ts", C.c_double),
-        ("n_pairs", C.c_int32), ("n_b", C.c_int32), ("n_dirs", C.c_int32), ("pad1", C.c_int32),
+        ("n_pairs", C.c_int32), ("n_b", C.c_int32), ("n_dirs", C.c_int32), ("min_blocks", C.c_int32),
         ("pair_jd", C.c_int32 * MADI_MAX_PAIRS), ("pair_jD", C.c_int32 * MADI_MAX_PAIRS),
         ("pair_js", C.c_int32 * MADI_MAX_PAIRS),
         ("coef", C.c_float * (MADI_MAX_PAIRS * MADI_MAX_B)),
@@ -119,6 +119,8 @@ def _declare(lib):
     lib.madi_walk.argtypes = [C.POINTER(MadiWalkDesc), P]
     lib.madi_walk_smem_bytes.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     lib.madi_walk_smem_bytes.restype = C.c_int64
+    lib.madi_walk_blocks_per_sm.argtypes = [C.POINTER(MadiWalkDesc)]
+    lib.madi_walk_blocks_per_sm.restype = C.c_int32
     lib.madi_reduce_Y.argtypes = [P, C.c_int64, C.c_int32, P, P, P, P, C.c_int32, P, P, P]
     lib.madi_match.argtypes = [C.POINTER(MadiMatchDesc), P]
     lib.madi_match_scratch_bytes.argtypes = [C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32]

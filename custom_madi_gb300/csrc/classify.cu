@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(128) classify_kernel(const madi_geometry gd, c
         path = 0;
         float rs;
         if (F32IN) {
-            st = classify_f32(g, (float)px, (float)py, (float)pz, seed, inside, rs);
+            st = classify_f32(g, (float)px, (float)py, (float)pz, -1, seed, inside, rs);
         } else {
             // fp64 input: the fp32 rule only sees rounded coordinates, so decide in fp64.
             st = CLS_FALLBACK;

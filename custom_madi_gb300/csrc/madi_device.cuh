@@ -45,11 +45,11 @@ MADI_DEV void box_muller(uint32_t a, uint32_t b, float& g0, float& g1) {
 
 // ---------------------------------------------------------------------------
 // Geometry view.  `base` is either shared memory (staged) or the global stage
-// buffer; both carry the same layout (madi_geometry in madi_gb300.h).
+// buffer; both carry the layout of madi_geometry (include/madi_gb300.h).
 // ---------------------------------------------------------------------------
 struct Geo {
-    const float4* hi;
-    const float4* lo;
+    const float4* seed;         // x, y, z (fp32), alpha (fp32)
+    const int32_t* cell;
     const uint32_t* off;
     const void* ids;
     const double* f64;          // [n][4] in global memory
@@ -60,13 +60,14 @@ struct Geo {
     float inv_h;
     float L;
     float cap;
+    float cerr;                 // |fp32 seed - exact seed| per axis
     int n_seeds;
 };
 
 MADI_DEV Geo make_geo(const madi_geometry& g, const unsigned char* base) {
     Geo v;
-    v.hi = reinterpret_cast<const float4*>(base);
-    v.lo = reinterpret_cast<const float4*>(base + g.off_seed_lo);
+    v.seed = reinterpret_cast<const float4*>(base);
+    v.cell = reinterpret_cast<const int32_t*>(base + g.off_cell);
     v.off = reinterpret_cast<const uint32_t*>(base + g.off_grid_offset);
     v.ids = base + g.off_grid_ids;
     v.f64 = g.seed_f64;
@@ -77,6 +78,7 @@ MADI_DEV Geo make_geo(const madi_geometry& g, const unsigned char* base) {
     v.inv_h = (float)(1.0 / g.grid_h);
     v.L = (float)g.L;
     v.cap = (float)g.safe_cap;
+    v.cerr = (float)g.coord_err;
     v.n_seeds = g.n_seeds;
     return v;
 }
@@ -94,78 +96,65 @@ MADI_DEV int voxel_of(const Geo& g, float px, float py, float pz) {
     return (iz * g.G + iy) * g.G + ix;
 }
 
-MADI_DEV int cell_of(const Geo& g, int seed) { return __float_as_int(g.lo[seed].w); }
+MADI_DEV int cell_of(const Geo& g, int seed) { return g.cell[seed]; }
 
-enum { CLS_OK = 0, CLS_FALLBACK = 1, CLS_ERROR = 2 };
+enum { CLS_OK = 0, CLS_FALLBACK = 1, CLS_ERROR = 2, CLS_NOT_NEAREST = 3 };
 
-// Relative error budget of the fp32 path (2^-17: about 64x the accumulated
-// rounding of the double-float seed differences, dot products and rsqrt).
-#define MADI_TOL_REL 7.62939453125e-06f
-#define MADI_TIE_REL 3.814697265625e-06f
+#define MADI_EPS21 4.76837158203125e-07f   // 2^-21
+#define MADI_EPS19 1.9073486328125e-06f    // 2^-19
 
 // ---------------------------------------------------------------------------
-// fp32 voxel-grid classifier.  Seeds are double-float (hi + lo) so p - c keeps a
-// relative (not box-relative) error.  Returns CLS_FALLBACK when the nearest seed
-// or a binding facet lies inside the error band; the caller then runs the fp64
-// rule on the same (proven superset) candidate list.
+// fp32 voxel-grid classifier.
+//
+// For nearest seed c1 the shifted-facet margin of p w.r.t. seed cj is the signed
+// distance of p to their bisector plane,  m_j = u.(cj + c1 - 2p) / (2|u|),
+// u = cj - c1, and p is intracellular iff m_j >= alpha_1 for every j.  The fp32
+// value carries the error bound
+//   tol_j = 2 [ e (1 + |w|/|u|) + 2^-21 (|p-c1| + |p-cj| + |w| + |m_j|) ],
+// w = 2p - cj - c1, e the per-axis fp32 seed rounding; decisions inside the
+// band go to the fp64 rule (CLS_FALLBACK).  The same pass proves nearestness:
+// m_j < 0 means cj is closer than c1 (CLS_NOT_NEAREST).
 //
 // rsafe receives a proven lower bound on the distance from p to the nearest
 // point whose label differs (capped at g.cap):
 //   inside : min_j (m_j - alpha_1)                   (distance to the shrunk facets)
 //   outside: min( alpha_1 - min_j m_j,               (distance to the own shrunk cell)
 //                 min_{i != 1} (m_i + alpha_i) )      (distance to any other shrunk cell)
-// Seeds absent from the list have m > alpha_max + cap, so they cannot lower it.
+// Seeds absent from the voxel list have m > alpha_max + cap, so they cannot lower it.
 // ---------------------------------------------------------------------------
-MADI_DEV int classify_f32(const Geo& g, float px, float py, float pz,
-                          int& seed1, int& inside, float& rsafe) {
-    const int v = voxel_of(g, px, py, pz);
-    const uint32_t b = g.off[v], e = g.off[v + 1];
-    if (b >= e) return CLS_ERROR;
-    float best = 3.0e38f, second = 3.0e38f;
-    int bi = -1;
-    for (uint32_t k = b; k < e; ++k) {
-        const int id = cand_id(g, k);
-        const float4 h = g.hi[id];
-        const float4 l = g.lo[id];
-        const float ax = (px - h.x) - l.x, ay = (py - h.y) - l.y, az = (pz - h.z) - l.z;
-        const float d2 = fmaf(ax, ax, fmaf(ay, ay, az * az));
-        if (d2 < best) { second = best; best = d2; bi = id; }
-        else if (d2 < second) { second = d2; }
-    }
-    if (second - best <= MADI_TIE_REL * second) return CLS_FALLBACK;
-    const float4 h1 = g.hi[bi];
-    const float4 l1 = g.lo[bi];
+MADI_DEV int margins_pass(const Geo& g, float px, float py, float pz, uint32_t b, uint32_t e, int bi,
+                          int& inside, float& rsafe) {
+    const float4 h1 = g.seed[bi];
     const float a1 = h1.w;
-    const float bx = (px - h1.x) - l1.x, by = (py - h1.y) - l1.y, bz = (pz - h1.z) - l1.z;
-    const float b1 = fabsf(bx) + fabsf(by) + fabsf(bz);
-    bool out_sure = false, amb = false;
-    float r_in = 3.0e38f, r_other = 3.0e38f;
-    float m_min_up = 3.0e38f;
+    const float bx = px - h1.x, by = py - h1.y, bz = pz - h1.z;
+    const float t0 = g.cerr + MADI_EPS21 * 3.0f * (fabsf(bx) + fabsf(by) + fabsf(bz));
+    bool out_sure = false, amb = false, found = false, tie = false;
+    float r_in = 3.0e38f, r_other = 3.0e38f, m_min_up = 3.0e38f;
     for (uint32_t k = b; k < e; ++k) {
         const int id = cand_id(g, k);
-        if (id == bi) continue;
-        const float4 h = g.hi[id];
-        const float4 l = g.lo[id];
-        const float ax = (px - h.x) - l.x, ay = (py - h.y) - l.y, az = (pz - h.z) - l.z;
-        const float ux = (h.x - h1.x) + (l.x - l1.x);
-        const float uy = (h.y - h1.y) + (l.y - l1.y);
-        const float uz = (h.z - h1.z) + (l.z - l1.z);
-        const float wx = ax + bx, wy = ay + by, wz = az + bz;
+        if (id == bi) { found = true; continue; }
+        const float4 h = g.seed[id];
+        const float ux = h.x - h1.x, uy = h.y - h1.y, uz = h.z - h1.z;
+        const float wx = (px - h.x) + bx, wy = (py - h.y) + by, wz = (pz - h.z) + bz;
         const float num = -fmaf(ux, wx, fmaf(uy, wy, uz * wz));
-        const float s2 = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
-        const float m = 0.5f * num * rsqrtf(s2);
-        const float tol = MADI_TOL_REL * (fabsf(ax) + fabsf(ay) + fabsf(az) + b1 + fabsf(m) + a1 + h.w);
+        const float rs = rsqrtf(fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
+        const float m = 0.5f * num * rs;
+        const float wl = fabsf(wx) + fabsf(wy) + fabsf(wz);
+        const float tol = 2.0f * (t0 + wl * fmaf(g.cerr, rs, 2.0f * MADI_EPS21) + MADI_EPS21 * (fabsf(m) + a1 + h.w));
+        if (m < -tol) return CLS_NOT_NEAREST;
         const float dm = m - a1;
         out_sure |= dm < -tol;
         amb |= fabsf(dm) <= tol;
         r_in = fminf(r_in, dm - tol);
         m_min_up = fminf(m_min_up, m + tol);
         r_other = fminf(r_other, m - tol + h.w);
+        tie |= m <= tol;                     // nearest seed not decided in fp32
     }
-    seed1 = bi;
+    if (!found) return CLS_NOT_NEAREST;
+    if (tie) return CLS_FALLBACK;
     if (out_sure) {
         inside = 0;
-        float r = fminf(a1 * (1.0f - MADI_TOL_REL) - m_min_up, r_other);
+        const float r = fminf(a1 * (1.0f - MADI_EPS19) - m_min_up, r_other);
         rsafe = fminf(fmaxf(r, 0.0f), g.cap);
         return CLS_OK;
     }
@@ -173,6 +162,176 @@ MADI_DEV int classify_f32(const Geo& g, float px, float py, float pz,
     inside = 1;
     rsafe = fminf(fmaxf(r_in, 0.0f), g.cap);
     return CLS_OK;
+}
+
+// guess: the nearest seed of a nearby earlier point (or -1).  One pass when the
+// guess is still nearest, else a nearest search over the list and a second pass.
+MADI_DEV int classify_f32(const Geo& g, float px, float py, float pz, int guess,
+                          int& seed1, int& inside, float& rsafe) {
+    const int v = voxel_of(g, px, py, pz);
+    const uint32_t b = g.off[v], e = g.off[v + 1];
+    if (b >= e) return CLS_ERROR;
+    if (guess >= 0) {
+        const int st = margins_pass(g, px, py, pz, b, e, guess, inside, rsafe);
+        if (st != CLS_NOT_NEAREST) { seed1 = guess; return st; }
+    }
+    float best = 3.0e38f, second = 3.0e38f;
+    int bi = -1;
+    for (uint32_t k = b; k < e; ++k) {
+        const int id = cand_id(g, k);
+        const float4 h = g.seed[id];
+        const float ax = px - h.x, ay = py - h.y, az = pz - h.z;
+        const float d2 = fmaf(ax, ax, fmaf(ay, ay, az * az));
+        if (d2 < best) { second = best; best = d2; bi = id; }
+        else if (d2 < second) { second = d2; }
+    }
+    if (second - best <= MADI_EPS19 * second + 8.0f * g.cerr * sqrtf(second)) return CLS_FALLBACK;
+    seed1 = bi;
+    const int st = margins_pass(g, px, py, pz, b, e, bi, inside, rsafe);
+    return st == CLS_NOT_NEAREST ? CLS_FALLBACK : st;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-cooperative form of classify_f32: the 32 lanes of a warp classify ONE
+// point together, lane l taking candidates b + l, b + l + 32, ... of its voxel
+// list, and combine with warp reductions.  Same arithmetic per candidate and
+// the same decisions as the per-lane form; every lane returns the same result.
+// Called in warp-uniform control flow only.
+// ---------------------------------------------------------------------------
+#define MADI_FULL 0xffffffffu
+
+// Order-preserving int image of a float, for integer warp min-reductions.
+MADI_DEV int f2o(float f) { const int i = __float_as_int(f); return i >= 0 ? i : i ^ 0x7FFFFFFF; }
+MADI_DEV float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
+MADI_DEV float warp_minf(float v) { return o2f(__reduce_min_sync(MADI_FULL, f2o(v))); }
+
+// Label cache proven at a classified point p (walker displacement frame):
+// j* = the seed with the smallest margin m_j* (the nearest shifted facet),
+// R   = min(cap, min_{j != 1, j*} (m_j(p) - alpha_1) - tol).
+// Every q with |q - p| < R is on c1's side of all other facets by more than
+// alpha_1 (margins are 1-Lipschitz), so its label follows from the one exact
+// plane m_j*(q) = off - n.q:  >= alpha_1 intracellular (cell of c1),
+// in (-alpha_j*, alpha_1) extracellular; anything else needs a new pass.
+// The thresholds include the fp32 error of the plane evaluation.
+struct SlabCache {
+    float nx, ny, nz, off;
+    float in_thr, gap_hi, gap_lo;
+    float R2;
+};
+
+MADI_DEV int coop_margins(const Geo& g, float px, float py, float pz, uint32_t b, uint32_t e, int bi, int lane,
+                          float ex, float ey, float ez, int& inside, SlabCache& sc) {
+    const float4 h1 = g.seed[bi];
+    const float a1 = h1.w;
+    const float bx = px - h1.x, by = py - h1.y, bz = pz - h1.z;
+    const float t0 = g.cerr + MADI_EPS21 * 3.0f * (fabsf(bx) + fabsf(by) + fabsf(bz));
+    bool not_near = false, out_sure = false, amb = false, found = false, tie = false;
+    // per lane: the candidate with the smallest margin, and the smallest (m - alpha_1 - tol)
+    // over all of its candidates (r_all) and over the others (r_excl)
+    float m_best = 3.0e38f, r_best = 3.0e38f, r_excl = 3.0e38f;
+    int j_best = -1;
+    for (uint32_t k = b + lane; k < e; k += 32) {
+        const int id = cand_id(g, k);
+        if (id == bi) { found = true; continue; }
+        const float4 h = g.seed[id];
+        const float ux = h.x - h1.x, uy = h.y - h1.y, uz = h.z - h1.z;
+        const float wx = (px - h.x) + bx, wy = (py - h.y) + by, wz = (pz - h.z) + bz;
+        const float num = -fmaf(ux, wx, fmaf(uy, wy, uz * wz));
+        const float rs = rsqrtf(fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
+        const float m = 0.5f * num * rs;
+        const float wl = fabsf(wx) + fabsf(wy) + fabsf(wz);
+        const float tol = 2.0f * (t0 + wl * fmaf(g.cerr, rs, 2.0f * MADI_EPS21) + MADI_EPS21 * (fabsf(m) + a1 + h.w));
+        const float dm = m - a1;
+        not_near |= m < -tol;
+        out_sure |= dm < -tol;
+        amb |= fabsf(dm) <= tol;
+        tie |= m <= tol;
+        const float r = dm - tol;
+        if (m < m_best) {
+            r_excl = fminf(r_excl, r_best);
+            m_best = m; r_best = r; j_best = id;
+        } else {
+            r_excl = fminf(r_excl, r);
+        }
+    }
+    sc.R2 = 0.f;
+    if (__any_sync(MADI_FULL, not_near) || !__any_sync(MADI_FULL, found)) return CLS_NOT_NEAREST;
+    if (__any_sync(MADI_FULL, tie)) return CLS_FALLBACK;
+    const bool outside = __any_sync(MADI_FULL, out_sure);
+    if (!outside && __any_sync(MADI_FULL, amb)) return CLS_FALLBACK;
+    inside = outside ? 0 : 1;
+    // j*: lane holding the smallest margin
+    const float mmin = warp_minf(m_best);
+    const unsigned who = __ballot_sync(MADI_FULL, m_best == mmin);
+    const int jl = __ffs(who) - 1;
+    const float rest = warp_minf(lane == jl ? r_excl : fminf(r_best, r_excl));
+    const int js = __shfl_sync(MADI_FULL, j_best, jl);
+    const float R = fminf(rest, g.cap);
+    if (R > 0.f && js >= 0) {
+        const float4 hj = g.seed[js];
+        const float ux = hj.x - h1.x, uy = hj.y - h1.y, uz = hj.z - h1.z;
+        const float rsj = rsqrtf(fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
+        const float nx = ux * rsj, ny = uy * rsj, nz = uz * rsj;
+        const float aj = hj.w;
+        // plane in the displacement frame: m(q) = |u|/2 - n.(q - c1), c1 at e + (c1 - p)
+        const float cx = ex - bx, cy = ey - by, cz = ez - bz;
+        const float hu = 0.5f / rsj;
+        sc.nx = nx; sc.ny = ny; sc.nz = nz;
+        sc.off = hu + fmaf(nx, cx, fmaf(ny, cy, nz * cz));
+        const float dist = fabsf(bx) + fabsf(by) + fabsf(bz) + R;
+        const float T = 2.0f * (g.cerr * (2.0f + 4.0f * dist * rsj)
+                                + MADI_EPS21 * (fabsf(ex) + fabsf(ey) + fabsf(ez) + fabsf(cx) + fabsf(cy) + fabsf(cz)
+                                                + 2.0f * dist + hu + a1 + aj));
+        sc.in_thr = a1 + T;
+        sc.gap_hi = a1 - T;
+        sc.gap_lo = -aj + T;
+        sc.R2 = R * R * (1.0f - MADI_EPS19);
+    }
+    return CLS_OK;
+}
+
+MADI_DEV int coop_nearest(const Geo& g, float px, float py, float pz, uint32_t b, uint32_t e, int lane, int& bi) {
+    float best = 3.0e38f, second = 3.0e38f;
+    int id_best = -1;
+    for (uint32_t k = b + lane; k < e; k += 32) {
+        const int id = cand_id(g, k);
+        const float4 h = g.seed[id];
+        const float ax = px - h.x, ay = py - h.y, az = pz - h.z;
+        const float d2 = fmaf(ax, ax, fmaf(ay, ay, az * az));
+        if (d2 < best) { second = best; best = d2; id_best = id; }
+        else if (d2 < second) { second = d2; }
+    }
+    // d2 >= 0, so the float bit patterns order like unsigned integers.
+    const unsigned key = __float_as_uint(best);
+    const unsigned kmin = __reduce_min_sync(MADI_FULL, key);
+    const unsigned who = __ballot_sync(MADI_FULL, key == kmin);
+    const int src = __ffs(who) - 1;
+    bi = __shfl_sync(MADI_FULL, id_best, src);
+    const float sec = lane == src ? second : best;
+    const float smin = __uint_as_float(__reduce_min_sync(MADI_FULL, __float_as_uint(sec)));
+    const float bmin = __uint_as_float(kmin);
+    if (__popc(who) > 1 || smin - bmin <= MADI_EPS19 * smin + 8.0f * g.cerr * sqrtf(smin)) return CLS_FALLBACK;
+    return CLS_OK;
+}
+
+// Classify point p (walker displacement e) cooperatively; guess = nearest seed
+// of an earlier nearby point or -1.  On CLS_OK sc holds the label cache.
+MADI_DEV int coop_classify(const Geo& g, float px, float py, float pz, float ex, float ey, float ez, int guess,
+                           int lane, int& seed1, int& inside, SlabCache& sc) {
+    sc.R2 = 0.f;
+    const int v = voxel_of(g, px, py, pz);
+    const uint32_t b = g.off[v], e = g.off[v + 1];
+    if (b >= e) return CLS_ERROR;
+    if (guess >= 0) {
+        const int st = coop_margins(g, px, py, pz, b, e, guess, lane, ex, ey, ez, inside, sc);
+        if (st != CLS_NOT_NEAREST) { seed1 = guess; return st; }
+    }
+    int bi = 0;
+    const int st = coop_nearest(g, px, py, pz, b, e, lane, bi);
+    if (st != CLS_OK) return st;
+    seed1 = bi;
+    const int st2 = coop_margins(g, px, py, pz, b, e, bi, lane, ex, ey, ez, inside, sc);
+    return st2 == CLS_NOT_NEAREST ? CLS_FALLBACK : st2;
 }
 
 // ---------------------------------------------------------------------------

@@ -31,19 +31,358 @@ MADI_DEV double y_ref(double yrel, double x0, double half_L, double t) {
     return yrel + (x0 - half_L) * t;
 }
 
-template <bool STAGED, int OUT, bool PERIODIC>
-__global__ void __launch_bounds__(256) walk_f32_kernel(const madi_walk_desc d) {
+// Shared-memory blocks of one CTA besides the staged geometry.
+struct TileShared {
+    long long* acc;       // [2 n_out] fixed-point cos / sin sums of the tile
+    unsigned int* occ;    // [n_grid] inside counts
+    const Snap* snap;     // [n_grid] moment coefficients
+    SlabCache* pend;      // [blockDim.x] label cache of this step's refresh, per walker
+    double* auxd;         // [3][blockDim.x] Y' at the last storage point (fp64)
+    float* auxf;          // [3 + 3 NP][blockDim.x] interval-start displacement, moments dM
+    uint32_t* auxc;       // [3][blockDim.x] rare counters: fp64 fallbacks, accepted, rejected crossings
+};
+
+// Per-walker state touched once per storage interval lives in shared memory
+// (structure of arrays, one column per thread) to keep the step loop in registers.
+#define AUX_Y(k) ts.auxd[(k) * blockDim.x + threadIdx.x]
+#define AUX_A(k) ts.auxf[(k) * blockDim.x + threadIdx.x]
+#define AUX_M(p, k) ts.auxf[(3 + 3 * (p) + (k)) * blockDim.x + threadIdx.x]
+#define AUX_C(k) ts.auxc[(k) * blockDim.x + threadIdx.x]
+
+// Walk one tile (blockDim.x walkers of one job) on geometry view g.
+template <int OUT, bool PERIODIC, int NP>
+__device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_walk_job& job,
+                                          const madi_geometry& gd, const Geo& g, int local, const TileShared& ts) {
+    const int lane = threadIdx.x & 31;
+    const bool active = local < job.n_walkers;
+    const uint32_t widx = job.walker_base + (uint32_t)local;
+    const float L = (float)gd.L;
+    const float sigma = (float)d.sigma;
+    const bool cells = gd.has_cells != 0;
+    const bool stream = d.rng == MADI_RNG_STREAM;
+
+    // ---- initial position (Omega_src cube; the whole box when periodic) ----
+    float px = 0.f, py = 0.f, pz = 0.f;
+    if (active) {
+        double x0, y0, z0;
+        if (stream) {
+            x0 = d.init[3 * (size_t)local + 0];
+            y0 = d.init[3 * (size_t)local + 1];
+            z0 = d.init[3 * (size_t)local + 2];
+        } else {
+            const U4 r = philox10(U4{widx, 0u, 0u, 1u}, job.key0, job.key1);
+            const double span = gd.source_hi - gd.source_lo;
+            x0 = gd.source_lo + span * ((double)r.x * 2.3283064365386963e-10);
+            y0 = gd.source_lo + span * ((double)r.y * 2.3283064365386963e-10);
+            z0 = gd.source_lo + span * ((double)r.z * 2.3283064365386963e-10);
+        }
+        px = (float)x0; py = (float)y0; pz = (float)z0;
+        if (PERIODIC) {
+            if (px >= L) px = 0.f;
+            if (py >= L) py = 0.f;
+            if (pz >= L) pz = 0.f;
+        }
+    }
+    const float x0f = px, y0f = py, z0f = pz;
+    // ---- state ----
+    float dx = 0.f, dy = 0.f, dz = 0.f;           // unwrapped displacement from x0
+    float rx = 0.f, ry = 0.f, rz = 0.f;           // label-cache centre (displacement frame)
+    SlabCache sc;
+    sc.R2 = 0.f; sc.nx = sc.ny = sc.nz = sc.off = sc.in_thr = sc.gap_hi = sc.gap_lo = 0.f;
+    int cell = 0, inside = 0, seed = -1;          // seed: nearest seed at the last classification
+    int cache_cell = 0;
+    bool dead = !active;
+    bool frozen = !active;
+    uint32_t n_full = 0, n_t1 = 0, escaped = 0, cerr = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { AUX_Y(k) = 0.0; AUX_A(k) = 0.f; AUX_C(k) = 0u; }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) { AUX_M(p, 0) = 0.f; AUX_M(p, 1) = 0.f; AUX_M(p, 2) = 0.f; }
+    if (cells) {
+        int my_st = CLS_OK, my_s1 = 0, my_in = 0;
+        for (unsigned pend = __ballot_sync(MADI_FULL, active); pend; pend &= pend - 1) {
+            const int src = __ffs(pend) - 1;
+            const float sx = __shfl_sync(MADI_FULL, px, src);
+            const float sy = __shfl_sync(MADI_FULL, py, src);
+            const float sz = __shfl_sync(MADI_FULL, pz, src);
+            int s1 = 0, in = 0;
+            SlabCache c;
+            const int st = coop_classify(g, sx, sy, sz, 0.f, 0.f, 0.f, -1, lane, s1, in, c);
+            if (lane == src) { my_st = st; my_s1 = s1; my_in = in; ts.pend[threadIdx.x] = c; }
+        }
+        __syncwarp();
+        if (active) {
+            if (my_st == CLS_FALLBACK) {
+                my_st = classify_list_f64(g, px, py, pz, my_s1, my_in);
+                ts.pend[threadIdx.x].R2 = 0.f;
+                ++AUX_C(0);
+            }
+            if (my_st != CLS_OK) { cerr = 1; dead = true; }
+            else { cell = cell_of(g, my_s1); inside = my_in; sc = ts.pend[threadIdx.x]; seed = my_s1; cache_cell = cell; }
+            ++n_full;
+        }
+    }
+    float Sx = 0.f, Sy = 0.f, Sz = 0.f;           // sum of displacements in this interval
+    const size_t row = (size_t)job.y_row + (size_t)local;
+    if (OUT == MADI_OUT_Y && active) {
+        d.Y[(row * d.n_grid) * 3 + 0] = 0.0;
+        d.Y[(row * d.n_grid) * 3 + 1] = 0.0;
+        d.Y[(row * d.n_grid) * 3 + 2] = 0.0;
+        d.inside_trace[row * d.n_grid] = (int8_t)inside;
+    }
+    {
+        const unsigned b = __ballot_sync(0xffffffffu, active && inside);
+        if (lane == 0 && b) atomicAdd(&ts.occ[0], (unsigned)__popc(b));
+    }
+    const bool always = job.pp >= 1.0;
+    const uint32_t th1 = (uint32_t)(job.thr1 >> 32), th2 = (uint32_t)(job.thr2 >> 32);
+    float g3 = 0.f, g4 = 0.f, g5 = 0.f;
+    uint32_t acc_word_odd = 0;
+    int h_left = d.steps_per_h;
+    int jgrid = 0;
+    for (int step = 0; step < d.n_steps; ++step) {
+        // ---- random numbers: one Philox call per step on average ----
+        float nx, ny, nz;
+        uint32_t word = 0;
+        double ustream = 0.0;
+        if (stream) {
+            if (!dead) {
+                const size_t o = ((size_t)step * job.n_walkers + local);
+                nx = (float)d.incr[3 * o + 0];
+                ny = (float)d.incr[3 * o + 1];
+                nz = (float)d.incr[3 * o + 2];
+                ustream = d.unif[o];
+            } else { nx = ny = nz = 0.f; }
+        } else if ((step & 1) == 0) {
+            const uint32_t pair = (uint32_t)step >> 1;
+            const U4 ra = philox10(U4{widx, pair, 0u, 0u}, job.key0, job.key1);
+            const U4 rb = philox10(U4{widx, pair, 1u, 0u}, job.key0, job.key1);
+            float g0, g1, g2;
+            box_muller(ra.x, ra.y, g0, g1);
+            box_muller(ra.z, ra.w, g2, g3);
+            box_muller(rb.x, rb.y, g4, g5);
+            nx = g0 * sigma; ny = g1 * sigma; nz = g2 * sigma;
+            word = rb.z;
+            acc_word_odd = rb.w;
+        } else {
+            nx = g3 * sigma; ny = g4 * sigma; nz = g5 * sigma;
+            word = acc_word_odd;
+        }
+        // ---- proposal and boundary ----
+        float qx = px, qy = py, qz = pz;
+        bool ok = false;
+        if (!dead) {
+            qx = px + nx; qy = py + ny; qz = pz + nz;
+            ok = true;
+            if (PERIODIC) {
+                if (qx < 0.f) qx += L;
+                if (qx >= L) qx -= L;
+                if (qy < 0.f) qy += L;
+                if (qy >= L) qy -= L;
+                if (qz < 0.f) qz += L;
+                if (qz >= L) qz -= L;
+            } else if (qx < 0.f || qx >= L || qy < 0.f || qy >= L || qz < 0.f || qz >= L) {
+                ok = false;
+                escaped = 1;
+                dead = true;
+            }
+        }
+        const float ex = dx + nx, ey = dy + ny, ez = dz + nz;
+        // ---- label cache: inside the proven sphere, one plane decides ----
+        bool t1 = false;
+        int t1_in = 0;
+        if (ok && cells) {
+            const float tx = ex - rx, ty = ey - ry, tz = ez - rz;
+            if (fmaf(tx, tx, fmaf(ty, ty, tz * tz)) < sc.R2) {
+                const float m = sc.off - fmaf(sc.nx, ex, fmaf(sc.ny, ey, sc.nz * ez));
+                if (m >= sc.in_thr) { t1 = true; t1_in = 1; }
+                else if (m < sc.gap_hi && m > sc.gap_lo) { t1 = true; t1_in = 0; }
+            }
+        }
+        // ---- full classifications of this step, one warp-cooperative pass each ----
+        const bool need = ok && cells && !t1;
+        int my_st = CLS_OK, my_s1 = 0, my_in = 0;
+        for (unsigned pend = __ballot_sync(MADI_FULL, need); pend; pend &= pend - 1) {
+            const int src = __ffs(pend) - 1;
+            const float sx = __shfl_sync(MADI_FULL, qx, src);
+            const float sy = __shfl_sync(MADI_FULL, qy, src);
+            const float sz = __shfl_sync(MADI_FULL, qz, src);
+            const float tx = __shfl_sync(MADI_FULL, ex, src);
+            const float ty = __shfl_sync(MADI_FULL, ey, src);
+            const float tz = __shfl_sync(MADI_FULL, ez, src);
+            const int sg = __shfl_sync(MADI_FULL, seed, src);
+            int s1 = 0, in = 0;
+            SlabCache c;
+            const int st = coop_classify(g, sx, sy, sz, tx, ty, tz, sg, lane, s1, in, c);
+            if (lane == src) { my_st = st; my_s1 = s1; my_in = in; ts.pend[threadIdx.x] = c; }
+        }
+        __syncwarp();
+        if (ok) {
+            int ncell = 0, nin = 0;
+            bool refreshed = false;
+            if (t1) {
+                ncell = cache_cell; nin = t1_in; ++n_t1;
+            } else if (need) {
+                if (my_st == CLS_FALLBACK) {
+                    my_st = classify_list_f64(g, qx, qy, qz, my_s1, my_in);
+                    ts.pend[threadIdx.x].R2 = 0.f;
+                    ++AUX_C(0);
+                }
+                ++n_full;
+                if (my_st != CLS_OK) { cerr = 1; dead = true; }
+                else { ncell = cell_of(g, my_s1); nin = my_in; refreshed = true; }
+            }
+            if (!dead) {
+                int m = 0;
+                if (inside != nin) m = 1;
+                else if (inside && nin && cell != ncell) m = 2;
+                bool accept = true;
+                if (m > 0 && !always) {
+                    if (stream) {
+                        accept = ustream < (m == 1 ? job.pp : job.pp * job.pp);
+                    } else {
+                        const uint32_t th = m == 1 ? th1 : th2;
+                        if (word != th) {
+                            accept = word < th;
+                        } else {
+                            const uint64_t thr = m == 1 ? job.thr1 : job.thr2;
+                            const U4 rc = philox10(U4{widx, (uint32_t)step, 2u, 0u}, job.key0, job.key1);
+                            accept = rc.x < (uint32_t)thr;
+                        }
+                    }
+                    ++AUX_C(accept ? 1 : 2);
+                }
+                if (accept) {
+                    px = qx; py = qy; pz = qz;
+                    dx = ex; dy = ey; dz = ez;
+                    cell = ncell; inside = nin;
+                    if (refreshed) { rx = ex; ry = ey; rz = ez; sc = ts.pend[threadIdx.x]; seed = my_s1; cache_cell = ncell; }
+                }
+            }
+        }
+        if (!dead) {
+            Sx += dx; Sy += dy; Sz += dz;
+        } else if (!frozen) {
+            // Walker stopped (fatal escape or classifier failure): close its
+            // trapezoid at the last accepted step and add nothing after.
+            frozen = true;
+            AUX_Y(0) += d.ts * ((double)Sx + 0.5 * ((double)AUX_A(0) - (double)dx));
+            AUX_Y(1) += d.ts * ((double)Sy + 0.5 * ((double)AUX_A(1) - (double)dy));
+            AUX_Y(2) += d.ts * ((double)Sz + 0.5 * ((double)AUX_A(2) - (double)dz));
+            Sx = Sy = Sz = 0.f;
+            AUX_A(0) = dx; AUX_A(1) = dy; AUX_A(2) = dz;
+        }
+        if (--h_left == 0) {
+            h_left = d.steps_per_h;
+            ++jgrid;
+            const double tsd = d.ts;
+            const double Yx = AUX_Y(0) + tsd * ((double)Sx + 0.5 * ((double)AUX_A(0) - (double)dx));
+            const double Yy = AUX_Y(1) + tsd * ((double)Sy + 0.5 * ((double)AUX_A(1) - (double)dy));
+            const double Yz = AUX_Y(2) + tsd * ((double)Sz + 0.5 * ((double)AUX_A(2) - (double)dz));
+            AUX_Y(0) = Yx; AUX_Y(1) = Yy; AUX_Y(2) = Yz;
+            Sx = Sy = Sz = 0.f;
+            AUX_A(0) = dx; AUX_A(1) = dy; AUX_A(2) = dz;
+            if (OUT == MADI_OUT_Y) {
+                if (active) {
+                    const double t = (double)jgrid * d.steps_per_h * tsd;
+                    const double half_L = 0.5 * gd.L;
+                    double* yo = d.Y + (row * d.n_grid + jgrid) * 3;
+                    yo[0] = y_ref(Yx, x0f, half_L, t);
+                    yo[1] = y_ref(Yy, y0f, half_L, t);
+                    yo[2] = y_ref(Yz, z0f, half_L, t);
+                    d.inside_trace[row * d.n_grid + jgrid] = (int8_t)inside;
+                }
+            } else {
+                const Snap sn = ts.snap[jgrid];
+                if (sn.any) {
+                    const float fx = (float)Yx, fy = (float)Yy, fz = (float)Yz;
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        const float k = snap_coef(sn.code, p);
+                        if (k != 0.f) {
+                            AUX_M(p, 0) = fmaf(k, fx, AUX_M(p, 0));
+                            AUX_M(p, 1) = fmaf(k, fy, AUX_M(p, 1));
+                            AUX_M(p, 2) = fmaf(k, fz, AUX_M(p, 2));
+                        }
+                    }
+                }
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, active && inside);
+            if (lane == 0 && b) atomicAdd(&ts.occ[jgrid], (unsigned)__popc(b));
+        }
+    }
+    // ---- phase epilogue: per (pair, dir, b) warp sums -> fixed point ----
+    if (OUT == MADI_OUT_FUSED) {
+        const bool live = active && !escaped && !cerr;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            if (p >= d.n_pairs) break;
+            const float mx = AUX_M(p, 0), my = AUX_M(p, 1), mz = AUX_M(p, 2);
+            for (int u = 0; u < d.n_dirs; ++u) {
+                const float proj = fmaf(d.dirs[3 * u], mx, fmaf(d.dirs[3 * u + 1], my, d.dirs[3 * u + 2] * mz));
+                for (int bb = 0; bb < d.n_b; ++bb) {
+                    float c = 0.f, s = 0.f;
+                    if (live) sincosf(d.coef[p * d.n_b + bb] * proj, &s, &c);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        c += __shfl_xor_sync(0xffffffffu, c, o);
+                        s += __shfl_xor_sync(0xffffffffu, s, o);
+                    }
+                    if (lane == 0) {
+                        const int idx = ((p * d.n_b + bb) * d.n_dirs + u) * 2;
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&ts.acc[idx]),
+                                  (unsigned long long)__float2ll_rn(c * 4294967296.0f));
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&ts.acc[idx + 1]),
+                                  (unsigned long long)__float2ll_rn(s * 4294967296.0f));
+                    }
+                }
+            }
+        }
+    }
+    // ---- counters ----
+    {
+        uint64_t* cnt = d.counters + (size_t)job.slot * MADI_CNT_N;
+        const uint32_t v0 = __reduce_add_sync(0xffffffffu, active ? 1u : 0u);
+        const uint32_t v1 = __reduce_add_sync(0xffffffffu, escaped);
+        const uint32_t v2 = __reduce_add_sync(0xffffffffu, cerr);
+        const uint32_t v3 = __reduce_add_sync(0xffffffffu, n_full);
+        const uint32_t v4 = __reduce_add_sync(0xffffffffu, n_t1);
+        const uint32_t v5 = __reduce_add_sync(0xffffffffu, AUX_C(0));
+        const uint32_t v6 = __reduce_add_sync(0xffffffffu, AUX_C(1));
+        const uint32_t v7 = __reduce_add_sync(0xffffffffu, AUX_C(2));
+        if (lane == 0) {
+            unsigned long long* c = reinterpret_cast<unsigned long long*>(cnt);
+            if (v0) atomicAdd(&c[0], (unsigned long long)v0);
+            if (v1) atomicAdd(&c[1], (unsigned long long)v1);
+            if (v2) atomicAdd(&c[2], (unsigned long long)v2);
+            if (v3) atomicAdd(&c[3], (unsigned long long)v3);
+            if (v4) atomicAdd(&c[4], (unsigned long long)v4);
+            if (v5) atomicAdd(&c[5], (unsigned long long)v5);
+            if (v6) atomicAdd(&c[6], (unsigned long long)v6);
+            if (v7) atomicAdd(&c[7], (unsigned long long)v7);
+        }
+    }
+}
+
+template <int OUT, bool PERIODIC, int NP, int MINB>
+__global__ void __launch_bounds__(256, MINB) walk_f32_kernel(const madi_walk_desc d) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_item;
     const int nthr = blockDim.x;
     const int tid = threadIdx.x;
-    const int lane = tid & 31;
     const int n_out = d.n_pairs * d.n_b * d.n_dirs;
     // Dynamic shared memory: [stage][acc int64 x 2 n_out][occ u32 x n_grid][snap x n_grid]
     unsigned char* stage = smem;
-    long long* acc = reinterpret_cast<long long*>(smem + d.stage_smem);
-    unsigned int* occ = reinterpret_cast<unsigned int*>(acc + 2 * n_out);
-    Snap* snap = reinterpret_cast<Snap*>(occ + d.n_grid);
+    TileShared ts;
+    ts.acc = reinterpret_cast<long long*>(smem + d.stage_smem);
+    ts.occ = reinterpret_cast<unsigned int*>(ts.acc + 2 * n_out);
+    Snap* snap = reinterpret_cast<Snap*>(ts.occ + d.n_grid);
+    ts.snap = snap;
+    unsigned char* aux = smem + d.stage_smem + 16 * n_out + 12 * ((d.n_grid + 3) & ~3);
+    ts.auxd = reinterpret_cast<double*>(aux);
+    ts.pend = reinterpret_cast<SlabCache*>(aux + 24 * nthr);
+    ts.auxf = reinterpret_cast<float*>(aux + 24 * nthr + (int)sizeof(SlabCache) * nthr);
+    ts.auxc = reinterpret_cast<uint32_t*>(ts.auxf + (3 + 3 * NP) * nthr);
 
     for (int j = tid; j < d.n_grid; j += nthr) {
         uint32_t code = 0, any = 0;
@@ -64,286 +403,38 @@ __global__ void __launch_bounds__(256) walk_f32_kernel(const madi_walk_desc d) {
             else s_item = first ? (int)blockIdx.x : d.n_tiles;
         }
         first = 0;
-        for (int i = tid; i < 2 * n_out; i += nthr) acc[i] = 0;
-        for (int j = tid; j < d.n_grid; j += nthr) occ[j] = 0;
+        for (int i = tid; i < 2 * n_out; i += nthr) ts.acc[i] = 0;
+        for (int j = tid; j < d.n_grid; j += nthr) ts.occ[j] = 0;
         __syncthreads();
         const int item = s_item;
         if (item >= d.n_tiles) break;
         const int jn = find_job(d.jobs, d.n_jobs, item);
         const madi_walk_job job = d.jobs[jn];
         const madi_geometry gd = d.geoms[job.geom];
-        if (STAGED && job.geom != cur_geom) {
-            const uint4* src = reinterpret_cast<const uint4*>(gd.stage);
-            uint4* dst = reinterpret_cast<uint4*>(stage);
-            for (uint32_t i = tid; i < gd.stage_bytes / 16u; i += nthr) dst[i] = src[i];
-            cur_geom = job.geom;
-            __syncthreads();
-        }
-        const Geo g = make_geo(gd, STAGED ? stage : reinterpret_cast<const unsigned char*>(gd.stage));
         const int local = (item - job.tile_begin) * nthr + tid;
-        const bool active = local < job.n_walkers;
-        const uint32_t widx = job.walker_base + (uint32_t)local;
-        const float L = (float)gd.L;
-        const float sigma = (float)d.sigma;
-        const bool cells = gd.has_cells != 0;
-        const bool stream = d.rng == MADI_RNG_STREAM;
-
-        // ---- initial position (Omega_src cube; the whole box when periodic) ----
-        float px = 0.f, py = 0.f, pz = 0.f;
-        double x0 = 0.0, y0 = 0.0, z0 = 0.0;
-        if (active) {
-            if (stream) {
-                x0 = d.init[3 * (size_t)local + 0];
-                y0 = d.init[3 * (size_t)local + 1];
-                z0 = d.init[3 * (size_t)local + 2];
-            } else {
-                const U4 r = philox10(U4{widx, 0u, 0u, 1u}, job.key0, job.key1);
-                const double span = gd.source_hi - gd.source_lo;
-                x0 = gd.source_lo + span * ((double)r.x * 2.3283064365386963e-10);
-                y0 = gd.source_lo + span * ((double)r.y * 2.3283064365386963e-10);
-                z0 = gd.source_lo + span * ((double)r.z * 2.3283064365386963e-10);
+        const bool here = d.stage_smem > 0 && (int)gd.stage_bytes <= d.stage_smem;
+        if (here) {
+            if (job.geom != cur_geom) {
+                const uint4* src = reinterpret_cast<const uint4*>(gd.stage);
+                uint4* dst = reinterpret_cast<uint4*>(stage);
+                for (uint32_t i = tid; i < gd.stage_bytes / 16u; i += nthr) dst[i] = src[i];
+                cur_geom = job.geom;
+                __syncthreads();
             }
-            px = (float)x0; py = (float)y0; pz = (float)z0;
-            if (PERIODIC) {
-                if (px >= L) px = 0.f;
-                if (py >= L) py = 0.f;
-                if (pz >= L) pz = 0.f;
-            }
-            x0 = px; y0 = py; z0 = pz;
-        }
-        // ---- state ----
-        float dx = 0.f, dy = 0.f, dz = 0.f;           // unwrapped displacement from x0
-        float rx = 0.f, ry = 0.f, rz = 0.f, r2 = 0.f; // Tier-1 sphere centre (displacement) and radius^2
-        int cell = 0, inside = 0;
-        bool dead = !active;
-        bool frozen = !active;
-        uint32_t n_full = 0, n_t1 = 0, n_fb = 0, n_acc = 0, n_rej = 0, escaped = 0, cerr = 0;
-        if (active && cells) {
-            int s1 = 0, in = 0;
-            float rs = 0.f;
-            int st = classify_f32(g, px, py, pz, s1, in, rs);
-            if (st == CLS_FALLBACK) { st = classify_list_f64(g, px, py, pz, s1, in); rs = 0.f; ++n_fb; }
-            if (st != CLS_OK) { cerr = 1; dead = true; }
-            cell = cell_of(g, s1); inside = in; r2 = rs * rs; ++n_full;
-        }
-        double Yx = 0.0, Yy = 0.0, Yz = 0.0;          // Y' at the last storage point
-        float Sx = 0.f, Sy = 0.f, Sz = 0.f;           // sum of displacements in this interval
-        float ax = 0.f, ay = 0.f, az = 0.f;           // displacement at the interval start
-        float dM[MADI_MAX_PAIRS][3];
-#pragma unroll
-        for (int p = 0; p < MADI_MAX_PAIRS; ++p) { dM[p][0] = dM[p][1] = dM[p][2] = 0.f; }
-        const size_t row = (size_t)job.y_row + (size_t)local;
-        if (OUT == MADI_OUT_Y && active) {
-            d.Y[(row * d.n_grid) * 3 + 0] = 0.0;
-            d.Y[(row * d.n_grid) * 3 + 1] = 0.0;
-            d.Y[(row * d.n_grid) * 3 + 2] = 0.0;
-            d.inside_trace[row * d.n_grid] = (int8_t)inside;
-        }
-        {
-            const unsigned b = __ballot_sync(0xffffffffu, active && inside);
-            if (lane == 0 && b) atomicAdd(&occ[0], (unsigned)__popc(b));
-        }
-        const double half_L = 0.5 * gd.L;
-        const uint64_t thr1 = job.thr1, thr2 = job.thr2;
-        const bool always = job.pp >= 1.0;
-        float g3 = 0.f, g4 = 0.f, g5 = 0.f;
-        uint32_t acc_word_odd = 0;
-        int h_left = d.steps_per_h;
-        int jgrid = 0;
-        for (int step = 0; step < d.n_steps; ++step) {
-            // ---- random numbers ----
-            float nx, ny, nz;
-            uint32_t word = 0;
-            double ustream = 0.0;
-            if (stream) {
-                if (!dead) {
-                    const size_t o = ((size_t)step * job.n_walkers + local);
-                    nx = (float)d.incr[3 * o + 0];
-                    ny = (float)d.incr[3 * o + 1];
-                    nz = (float)d.incr[3 * o + 2];
-                    ustream = d.unif[o];
-                } else { nx = ny = nz = 0.f; }
-            } else if ((step & 1) == 0) {
-                const uint32_t pair = (uint32_t)step >> 1;
-                const U4 ra = philox10(U4{widx, pair, 0u, 0u}, job.key0, job.key1);
-                const U4 rb = philox10(U4{widx, pair, 1u, 0u}, job.key0, job.key1);
-                float g0, g1, g2;
-                box_muller(ra.x, ra.y, g0, g1);
-                box_muller(ra.z, ra.w, g2, g3);
-                box_muller(rb.x, rb.y, g4, g5);
-                nx = g0 * sigma; ny = g1 * sigma; nz = g2 * sigma;
-                word = rb.z;
-                acc_word_odd = rb.w;
-            } else {
-                nx = g3 * sigma; ny = g4 * sigma; nz = g5 * sigma;
-                word = acc_word_odd;
-            }
-            if (!dead) {
-                float qx = px + nx, qy = py + ny, qz = pz + nz;
-                bool ok = true;
-                if (PERIODIC) {
-                    if (qx < 0.f) qx += L;
-                    if (qx >= L) qx -= L;
-                    if (qy < 0.f) qy += L;
-                    if (qy >= L) qy -= L;
-                    if (qz < 0.f) qz += L;
-                    if (qz >= L) qz -= L;
-                } else if (qx < 0.f || qx >= L || qy < 0.f || qy >= L || qz < 0.f || qz >= L) {
-                    ok = false;
-                    escaped = 1;
-                    dead = true;
-                }
-                if (ok) {
-                    const float ex = dx + nx, ey = dy + ny, ez = dz + nz;
-                    int ncell = 0, nin = 0;
-                    bool refreshed = false;
-                    float nr2 = 0.f;
-                    if (cells) {
-                        const float tx = ex - rx, ty = ey - ry, tz = ez - rz;
-                        const float disp2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
-                        if (disp2 < r2) {
-                            ncell = cell; nin = inside; ++n_t1;
-                        } else {
-                            int s1 = 0, in = 0;
-                            float rs = 0.f;
-                            int st = classify_f32(g, qx, qy, qz, s1, in, rs);
-                            if (st == CLS_FALLBACK) {
-                                st = classify_list_f64(g, qx, qy, qz, s1, in);
-                                rs = 0.f;
-                                ++n_fb;
-                            }
-                            ++n_full;
-                            if (st != CLS_OK) { cerr = 1; dead = true; }
-                            ncell = cell_of(g, s1); nin = in; nr2 = rs * rs; refreshed = true;
-                        }
-                    }
-                    if (!dead) {
-                        int m = 0;
-                        if (inside != nin) m = 1;
-                        else if (inside && nin && cell != ncell) m = 2;
-                        bool accept = true;
-                        if (m > 0 && !always) {
-                            if (stream) {
-                                const double thr = m == 1 ? job.pp : job.pp * job.pp;
-                                accept = ustream < thr;
-                            } else {
-                                const uint64_t thr = m == 1 ? thr1 : thr2;
-                                const uint32_t th = (uint32_t)(thr >> 32);
-                                if (word != th) {
-                                    accept = word < th;
-                                } else {
-                                    const U4 rc = philox10(U4{widx, (uint32_t)step, 2u, 0u}, job.key0, job.key1);
-                                    accept = rc.x < (uint32_t)thr;
-                                }
-                            }
-                            if (accept) ++n_acc; else ++n_rej;
-                        }
-                        if (accept) {
-                            px = qx; py = qy; pz = qz;
-                            dx = ex; dy = ey; dz = ez;
-                            cell = ncell; inside = nin;
-                            if (refreshed) { rx = ex; ry = ey; rz = ez; r2 = nr2; }
-                        }
-                    }
-                }
-            }
-            if (!dead) {
-                Sx += dx; Sy += dy; Sz += dz;
-            } else if (!frozen) {
-                // Walker stopped (fatal escape or classifier failure): close its
-                // trapezoid at the last accepted step and add nothing after.
-                frozen = true;
-                Yx += d.ts * ((double)Sx + 0.5 * ((double)ax - (double)dx));
-                Yy += d.ts * ((double)Sy + 0.5 * ((double)ay - (double)dy));
-                Yz += d.ts * ((double)Sz + 0.5 * ((double)az - (double)dz));
-                Sx = Sy = Sz = 0.f;
-                ax = dx; ay = dy; az = dz;
-            }
-            if (--h_left == 0) {
-                h_left = d.steps_per_h;
-                ++jgrid;
-                const double ts = d.ts;
-                Yx += ts * ((double)Sx + 0.5 * ((double)ax - (double)dx));
-                Yy += ts * ((double)Sy + 0.5 * ((double)ay - (double)dy));
-                Yz += ts * ((double)Sz + 0.5 * ((double)az - (double)dz));
-                Sx = Sy = Sz = 0.f;
-                ax = dx; ay = dy; az = dz;
-                if (OUT == MADI_OUT_Y) {
-                    if (active) {
-                        const double t = (double)jgrid * d.steps_per_h * ts;
-                        double* yo = d.Y + (row * d.n_grid + jgrid) * 3;
-                        yo[0] = y_ref(Yx, x0, half_L, t);
-                        yo[1] = y_ref(Yy, y0, half_L, t);
-                        yo[2] = y_ref(Yz, z0, half_L, t);
-                        d.inside_trace[row * d.n_grid + jgrid] = (int8_t)inside;
-                    }
-                } else {
-                    const Snap sn = snap[jgrid];
-                    if (sn.any) {
-                        const float fx = (float)Yx, fy = (float)Yy, fz = (float)Yz;
-#pragma unroll
-                        for (int p = 0; p < MADI_MAX_PAIRS; ++p) {
-                            const float k = snap_coef(sn.code, p);
-                            if (k != 0.f) {
-                                dM[p][0] = fmaf(k, fx, dM[p][0]);
-                                dM[p][1] = fmaf(k, fy, dM[p][1]);
-                                dM[p][2] = fmaf(k, fz, dM[p][2]);
-                            }
-                        }
-                    }
-                }
-                const unsigned b = __ballot_sync(0xffffffffu, active && inside);
-                if (lane == 0 && b) atomicAdd(&occ[jgrid], (unsigned)__popc(b));
-            }
-        }
-        // ---- phase epilogue: per (pair, dir, b) warp sums -> fixed point ----
-        if (OUT == MADI_OUT_FUSED) {
-            const bool live = active && !escaped && !cerr;
-            for (int p = 0; p < d.n_pairs; ++p) {
-                float mx = 0.f, my = 0.f, mz = 0.f;
-#pragma unroll
-                for (int q = 0; q < MADI_MAX_PAIRS; ++q)
-                    if (q == p) { mx = dM[q][0]; my = dM[q][1]; mz = dM[q][2]; }
-                for (int u = 0; u < d.n_dirs; ++u) {
-                    const float proj = fmaf(d.dirs[3 * u], mx, fmaf(d.dirs[3 * u + 1], my, d.dirs[3 * u + 2] * mz));
-                    for (int bb = 0; bb < d.n_b; ++bb) {
-                        float c = 0.f, s = 0.f;
-                        if (live) sincosf(d.coef[p * d.n_b + bb] * proj, &s, &c);
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) {
-                            c += __shfl_xor_sync(0xffffffffu, c, o);
-                            s += __shfl_xor_sync(0xffffffffu, s, o);
-                        }
-                        if (lane == 0) {
-                            const int idx = ((p * d.n_b + bb) * d.n_dirs + u) * 2;
-                            atomicAdd(reinterpret_cast<unsigned long long*>(&acc[idx]),
-                                      (unsigned long long)__float2ll_rn(c * 4294967296.0f));
-                            atomicAdd(reinterpret_cast<unsigned long long*>(&acc[idx + 1]),
-                                      (unsigned long long)__float2ll_rn(s * 4294967296.0f));
-                        }
-                    }
-                }
-            }
-        }
-        // ---- counters ----
-        {
-            uint32_t v[8] = {active ? 1u : 0u, escaped, cerr, n_full, n_t1, n_fb, n_acc, n_rej};
-            uint64_t* cnt = d.counters + (size_t)job.slot * MADI_CNT_N;
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const uint32_t s = __reduce_add_sync(0xffffffffu, v[i]);
-                if (lane == 0 && s) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[i]), (unsigned long long)s);
-            }
+            walk_tile<OUT, PERIODIC, NP>(d, job, gd, make_geo(gd, stage), local, ts);
+        } else {
+            walk_tile<OUT, PERIODIC, NP>(d, job, gd, make_geo(gd, reinterpret_cast<const unsigned char*>(gd.stage)),
+                                         local, ts);
         }
         __syncthreads();
         if (OUT == MADI_OUT_FUSED) {
             long long* out = reinterpret_cast<long long*>(d.accum) + (size_t)job.slot * 2 * n_out;
             for (int i = tid; i < 2 * n_out; i += nthr)
-                if (acc[i]) atomicAdd(reinterpret_cast<unsigned long long*>(&out[i]), (unsigned long long)acc[i]);
+                if (ts.acc[i]) atomicAdd(reinterpret_cast<unsigned long long*>(&out[i]), (unsigned long long)ts.acc[i]);
         }
         uint64_t* occ_out = d.occupancy + (size_t)job.slot * d.n_grid;
         for (int j = tid; j < d.n_grid; j += nthr)
-            if (occ[j]) atomicAdd(reinterpret_cast<unsigned long long*>(&occ_out[j]), (unsigned long long)occ[j]);
+            if (ts.occ[j]) atomicAdd(reinterpret_cast<unsigned long long*>(&occ_out[j]), (unsigned long long)ts.occ[j]);
     }
 }
 
@@ -368,7 +459,7 @@ __global__ void __launch_bounds__(128) walk_f64_kernel(const madi_walk_desc d) {
     if (cells) {
         int s1 = 0;
         if (classify_kd_f64(g, px, py, pz, s1, inside) != CLS_OK) cerr = 1;
-        cell = __float_as_int(g.lo[s1].w);
+        cell = g.cell[s1];
         ++n_full;
     }
     int kx = 0, ky = 0, kz = 0;
@@ -402,7 +493,7 @@ __global__ void __launch_bounds__(128) walk_f64_kernel(const madi_walk_desc d) {
                 if (cells) {
                     int s1 = 0;
                     if (classify_kd_f64(g, qx, qy, qz, s1, nin) != CLS_OK) { cerr = 1; }
-                    ncell = __float_as_int(g.lo[s1].w);
+                    ncell = g.cell[s1];
                     ++n_full;
                 }
                 if (!cerr) {
@@ -498,15 +589,16 @@ extern "C" int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walker
     return (int64_t)((stage_bytes + 15) & ~15) + acc + 4ll * n_grid + 8ll * n_grid + 16;
 }
 
-static int64_t fused_smem(const madi_walk_desc* d) {
+static int64_t fused_smem(const madi_walk_desc* d, int np) {
     const int64_t n_out = (int64_t)d->n_pairs * d->n_b * d->n_dirs;
-    return (int64_t)d->stage_smem + 16ll * n_out + 4ll * d->n_grid + 8ll * d->n_grid + 16;
+    return (int64_t)d->stage_smem + 16ll * n_out + 12ll * ((d->n_grid + 3) & ~3) +
+           ((int64_t)sizeof(SlabCache) + 24 + 4 * (3 + 3 * np) + 12) * d->tile_walkers;
 }
 
-template <bool STAGED, int OUT, bool PER>
+template <int OUT, bool PER, int NP, int MINB>
 static madi_status launch_f32(const madi_walk_desc* d, cudaStream_t s) {
-    auto k = walk_f32_kernel<STAGED, OUT, PER>;
-    const int64_t sm = fused_smem(d);
+    auto k = walk_f32_kernel<OUT, PER, NP, MINB>;
+    const int64_t sm = fused_smem(d, NP);
     if (sm > 227 * 1024) return host::fail(MADI_ERR_CAPACITY, "walker shared memory %lld B exceeds 227 KB", (long long)sm);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return host::cuda_fail(e, "cudaFuncSetAttribute(walker)");
@@ -515,6 +607,36 @@ static madi_status launch_f32(const madi_walk_desc* d, cudaStream_t s) {
     e = cudaGetLastError();
     if (e != cudaSuccess) return host::cuda_fail(e, "walker launch");
     return MADI_OK;
+}
+
+template <int OUT, bool PER>
+static madi_status launch_np(const madi_walk_desc* d, cudaStream_t s) {
+    const bool two = d->min_blocks >= 2;
+    if (OUT == MADI_OUT_FUSED && d->n_pairs > 4)
+        return two ? launch_f32<OUT, PER, 8, 2>(d, s) : launch_f32<OUT, PER, 8, 1>(d, s);
+    return two ? launch_f32<OUT, PER, 4, 2>(d, s) : launch_f32<OUT, PER, 4, 1>(d, s);
+}
+
+template <int OUT, bool PER>
+static const void* kernel_for(const madi_walk_desc* d) {
+    const bool two = d->min_blocks >= 2;
+    if (OUT == MADI_OUT_FUSED && d->n_pairs > 4)
+        return two ? (const void*)walk_f32_kernel<OUT, PER, 8, 2> : (const void*)walk_f32_kernel<OUT, PER, 8, 1>;
+    return two ? (const void*)walk_f32_kernel<OUT, PER, 4, 2> : (const void*)walk_f32_kernel<OUT, PER, 4, 1>;
+}
+
+extern "C" int32_t madi_walk_blocks_per_sm(const madi_walk_desc* d) {
+    if (!d || d->tile_walkers <= 0) return 0;
+    const bool per = d->boundary == MADI_BOUNDARY_PERIODIC;
+    const void* k = d->out_mode == MADI_OUT_FUSED
+        ? (per ? kernel_for<MADI_OUT_FUSED, true>(d) : kernel_for<MADI_OUT_FUSED, false>(d))
+        : (per ? kernel_for<MADI_OUT_Y, true>(d) : kernel_for<MADI_OUT_Y, false>(d));
+    const bool big = d->out_mode == MADI_OUT_FUSED && d->n_pairs > 4;
+    const int64_t sm = fused_smem(d, big ? 8 : 4);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, d->tile_walkers, (size_t)sm) != cudaSuccess) return 0;
+    return n;
 }
 
 extern "C" madi_status madi_walk(const madi_walk_desc* d, void* stream) {
@@ -564,17 +686,10 @@ extern "C" madi_status madi_walk(const madi_walk_desc* d, void* stream) {
         return host::fail(MADI_ERR_INVALID, "unknown out_mode");
     }
     if (d->stage_smem < 0 || (d->stage_smem & 15)) return host::fail(MADI_ERR_INVALID, "stage_smem must be a multiple of 16");
-    const bool staged = d->stage_smem > 0;
     const bool per = d->boundary == MADI_BOUNDARY_PERIODIC;
-    madi_status st;
-    if (d->out_mode == MADI_OUT_FUSED) {
-        if (staged) st = per ? launch_f32<true, MADI_OUT_FUSED, true>(d, s) : launch_f32<true, MADI_OUT_FUSED, false>(d, s);
-        else st = per ? launch_f32<false, MADI_OUT_FUSED, true>(d, s) : launch_f32<false, MADI_OUT_FUSED, false>(d, s);
-    } else {
-        if (staged) st = per ? launch_f32<true, MADI_OUT_Y, true>(d, s) : launch_f32<true, MADI_OUT_Y, false>(d, s);
-        else st = per ? launch_f32<false, MADI_OUT_Y, true>(d, s) : launch_f32<false, MADI_OUT_Y, false>(d, s);
-    }
-    return st;
+    if (d->out_mode == MADI_OUT_FUSED)
+        return per ? launch_np<MADI_OUT_FUSED, true>(d, s) : launch_np<MADI_OUT_FUSED, false>(d, s);
+    return per ? launch_np<MADI_OUT_Y, true>(d, s) : launch_np<MADI_OUT_Y, false>(d, s);
 }
 
 extern "C" madi_status madi_reduce_Y(const double* Y, int64_t n_walkers, int32_t n_grid, const int32_t* jd,

@@ -363,9 +363,9 @@ class DeviceGeometry:
         xyza[:, :3] = seeds
         xyza[:, 3] = ann
         hi = xyza.astype(np.float32)
-        lo = np.zeros((n, 4), np.float32)
-        lo[:, :3] = (seeds - hi[:, :3].astype(np.float64)).astype(np.float32)
-        lo[:, 3] = cellid.view(np.float32)
+        # per-axis bound on |fp32 seed - fp64 seed| (2x the half-ulp at the largest coordinate)
+        self.coord_err = float(np.max(np.abs(seeds - hi[:, :3].astype(np.float64)))) * 2.0 + \
+            2.0 ** -24 * float(np.max(np.abs(seeds))) if n else 0.0
         if ens.is_free_water:
             G, h, offsets, ids, u32 = 1, max(ens.L, 1.0), np.zeros(2, np.uint32), np.zeros(0, np.uint16), False
         else:
@@ -378,9 +378,9 @@ class DeviceGeometry:
         def pad16(b: bytes) -> bytes:
             return b + b"\0" * ((-len(b)) % 16)
 
-        parts = [hi.tobytes(), lo.tobytes(), pad16(offsets.tobytes()), pad16(ids.tobytes())]
-        off_lo = len(parts[0])
-        off_go = off_lo + len(parts[1])
+        parts = [hi.tobytes(), pad16(cellid.tobytes()), pad16(offsets.tobytes()), pad16(ids.tobytes())]
+        off_cell = len(parts[0])
+        off_go = off_cell + len(parts[1])
         off_gi = off_go + len(parts[2])
         blob = b"".join(parts)
         self.stage = torch.frombuffer(bytearray(blob), dtype=torch.uint8).to(device)
@@ -393,7 +393,7 @@ class DeviceGeometry:
         s.stage = N.ptr(self.stage)
         s.seed_f64 = N.ptr(self.seed_f64)
         s.kd_seed, s.kd_left, s.kd_right, s.kd_parent, s.kd_axis = [N.ptr(t) for t in self.kd]
-        s.off_seed_lo, s.off_grid_offset, s.off_grid_ids = off_lo, off_go, off_gi
+        s.off_cell, s.off_grid_offset, s.off_grid_ids = off_cell, off_go, off_gi
         s.stage_bytes = len(blob)
         s.n_seeds = n
         s.grid_n = G
@@ -405,6 +405,7 @@ class DeviceGeometry:
         s.safe_cap = float(ens.safe_cap)
         s.source_lo = float(ens.source_lo)
         s.source_hi = float(ens.source_hi)
+        s.coord_err = self.coord_err
         self.struct = s
         self.stage_bytes = len(blob)
 

@@ -237,7 +237,9 @@ class LaunchConfig:
     tile_walkers: int = 128
     blocks_per_sm: int = 0          # 0 = occupancy-derived
     persistent: bool = True
-    staged: Optional[bool] = None   # None = stage when it fits
+    staged: Optional[bool] = None   # False = always read geometry in place
+    stage_budget: int = 48 * 1024   # largest geometry staged into shared memory
+    min_blocks: int = 2             # register budget: 2 -> 128 registers/thread, 1 -> 255
 
 
 class WalkBatch:
@@ -300,6 +302,7 @@ class WalkBatch:
         d.out_mode = out_mode
         d.n_steps, d.steps_per_h, d.n_grid = cfg.n_steps, cfg.steps_per_h, cfg.n_grid
         d.sigma, d.ts = cfg.sigma, cfg.ts
+        d.min_blocks = int(lc.min_blocks)
         u = np.eye(3) if dirs is None else np.asarray(dirs, np.float64)
         self.n_dirs = len(u)
         self.layout = layout
@@ -337,17 +340,17 @@ class WalkBatch:
             d.init, d.incr, d.unif = N.ptr(self.s_init), N.ptr(self.s_incr), N.ptr(self.s_unif)
         if precision == 64:
             d.n_tiles = (int(self.jobs[0].n_walkers) + 127) // 128
-        # shared-memory staging and persistent grid
-        stage = max(g.stage_bytes for g in geoms)
-        stage = (stage + 15) // 16 * 16
-        fused_extra = 16 * self.n_out + 12 * cfg.n_grid + 16
-        want_stage = lc.staged if lc.staged is not None else (stage + fused_extra <= 200 * 1024)
-        d.stage_smem = stage if (want_stage and stage + fused_extra <= 227 * 1024) else 0
+        # shared-memory staging (every geometry that fits the per-CTA budget) and persistent grid
+        budget = lc.stage_budget if lc.staged is not False else 0
+        np_ = 8 if (layout is not None and layout.n_pairs > 4) else 4
+        fused_extra = 16 * self.n_out + 12 * ((cfg.n_grid + 3) // 4 * 4) + (32 + 24 + 4 * (3 + 3 * np_) + 12) * tw
+        fits = [g.stage_bytes for g in geoms if g.stage_bytes + fused_extra <= min(budget, 227 * 1024)]
+        d.stage_smem = ((max(fits) + 15) // 16 * 16) if (fits and precision == 32) else 0
         self.smem_bytes = d.stage_smem + fused_extra
+        self.staged_fraction = float(np.mean([g.stage_bytes <= d.stage_smem for g in geoms])) if d.stage_smem else 0.0
         sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         if lc.persistent and precision == 32:
-            bps = lc.blocks_per_sm or max(1, min(8, (228 * 1024) // max(self.smem_bytes + 1024, 1),
-                                              2048 // tw))
+            bps = lc.blocks_per_sm or max(1, int(N.lib().madi_walk_blocks_per_sm(C.byref(d))))
             d.grid_blocks = int(min(tiles, sms * bps))
         else:
             d.grid_blocks = 0
@@ -365,6 +368,31 @@ class WalkBatch:
 
     def counters_np(self) -> np.ndarray:
         return self.counters.cpu().numpy()
+
+    def _inputs(self) -> list:
+        ins = [self.geom_table, self.job_table]
+        for g in self.geoms:
+            ins += [g.stage, g.seed_f64, *g.kd]
+        return ins
+
+    def host_mirror(self) -> dict:
+        """Pinned host copies of every input buffer and pinned output buffers."""
+        ins = [t.cpu().pin_memory() for t in self._inputs()]
+        outs = [torch.empty(t.shape, dtype=t.dtype).pin_memory() for t in (self.accum, self.occupancy, self.counters)]
+        return {"inputs": ins, "outputs": outs,
+                "h2d_bytes": sum(t.numel() * t.element_size() for t in ins),
+                "d2h_bytes": sum(t.numel() * t.element_size() for t in outs)}
+
+    def run_from_host(self, host: dict) -> tuple:
+        """End-to-end call: host inputs -> device, walk, device sums -> host (synchronous)."""
+        s = torch.cuda.current_stream(self.dev)
+        for dst, src in zip(self._inputs(), host["inputs"]):
+            dst.copy_(src, non_blocking=True)
+        self.launch(s)
+        for src, dst in zip((self.accum, self.occupancy, self.counters), host["outputs"]):
+            dst.copy_(src, non_blocking=True)
+        s.synchronize()
+        return tuple(host["outputs"])
 
     def results(self) -> list:
         """Per job: dict(cos [n_cols, n_dirs], sin, occupancy, counters)."""

@@ -50,8 +50,8 @@ enum { MADI_BOUNDARY_FATAL = 0, MADI_BOUNDARY_PERIODIC = 1 };
  *
  *   stage  -- 16-byte aligned block copied whole into shared memory by the
  *             walker when stage_bytes fits; otherwise read in place.
- *             [ seed_hi : float4 x n_seeds ]  x,y,z rounded to fp32, w = alpha (fp32)
- *             [ seed_lo : float4 x n_seeds ]  x,y,z residuals (x - hi), w = cell id bits
+ *             [ seed : float4 x n_seeds ]  x,y,z rounded to fp32, w = alpha (fp32)
+ *             [ cell : int32 x n_seeds, padded to 16 bytes ]  base cell id of each seed
  *             [ grid_offset : uint32 x (G^3 + 1), padded to 16 bytes ]
  *             [ grid_ids : uint16 (or uint32 when ids_u32) x grid_total, padded ]
  *   seed_f64 -- double4 x n_seeds: x, y, z, alpha (the exact geometry).
@@ -71,7 +71,7 @@ typedef struct madi_geometry {
     const int32_t* kd_right;       /* device, [n_seeds]                           */
     const int32_t* kd_parent;      /* device, [n_seeds]                           */
     const int8_t*  kd_axis;        /* device, [n_seeds]                           */
-    uint32_t off_seed_lo;          /* byte offsets inside stage                   */
+    uint32_t off_cell;             /* byte offsets inside stage                   */
     uint32_t off_grid_offset;
     uint32_t off_grid_ids;
     uint32_t stage_bytes;          /* multiple of 16                              */
@@ -86,6 +86,7 @@ typedef struct madi_geometry {
     double   safe_cap;             /* Tier-1 radius cap the lists were built for  */
     double   source_lo;            /* walkers start uniform in [lo, hi)^3         */
     double   source_hi;
+    double   coord_err;            /* bound on |fp32 seed - fp64 seed| per axis   */
 } madi_geometry;
 
 /* Replaces Ensemble.classify_cpu (madi/ensemble.py:213-256) and the device
@@ -168,7 +169,8 @@ typedef struct madi_walk_desc {
     int32_t n_steps, steps_per_h, n_grid;
     double  sigma, ts;
     /* fused epilogue */
-    int32_t n_pairs, n_b, n_dirs, pad1;
+    int32_t n_pairs, n_b, n_dirs;
+    int32_t min_blocks;            /* register budget: 1 = 255 regs, 2 = 128 regs/thread */
     int32_t pair_jd[MADI_MAX_PAIRS], pair_jD[MADI_MAX_PAIRS], pair_js[MADI_MAX_PAIRS];
     float   coef[MADI_MAX_PAIRS * MADI_MAX_B];   /* phase coefficient per (pair, b)  */
     float   dirs[MADI_MAX_DIRS * 3];
@@ -190,6 +192,10 @@ madi_status madi_walk(const madi_walk_desc* desc, void* stream);
 
 /* Shared-memory bytes the fp32 walker needs for a geometry of stage_bytes. */
 int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walkers, int32_t n_grid);
+
+/* Resident CTAs per SM of the fp32 walker for this descriptor's shape
+ * (tile_walkers threads, stage_smem + epilogue shared memory); 0 on error. */
+int32_t madi_walk_blocks_per_sm(const madi_walk_desc* desc);
 
 /* Replaces _reduce_kernel (madi/walker_gpu.py:658-695) for grids too large for
  * the fused epilogue: Y [n_walkers][n_grid][3] fp64 -> cos_sum / sin_sum
