@@ -43,7 +43,7 @@ MADI_CNT_N = len(CNT_NAMES)
 EXPORTED = (
     "madi_abi_version", "madi_last_error_string", "madi_classify", "madi_walk",
     "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_scratch_bytes",
-    "madi_kdtree_build", "madi_grid_build", "madi_walk_blocks_per_sm",
+    "madi_kdtree_build", "madi_grid_build", "madi_walk_blocks_per_sm", "madi_walk_noalloc",
 )
 
 
@@ -117,6 +117,7 @@ def _declare(lib):
     lib.madi_last_error_string.restype = C.c_char_p
     lib.madi_classify.argtypes = [C.POINTER(MadiGeometry), P, C.c_int, C.c_int64, C.c_int, P, P, P, P]
     lib.madi_walk.argtypes = [C.POINTER(MadiWalkDesc), P]
+    lib.madi_walk_noalloc.argtypes = [C.POINTER(MadiWalkDesc), P]
     lib.madi_walk_smem_bytes.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     lib.madi_walk_smem_bytes.restype = C.c_int64
     lib.madi_walk_blocks_per_sm.argtypes = [C.POINTER(MadiWalkDesc)]
@@ -128,7 +129,7 @@ def _declare(lib):
     lib.madi_kdtree_build.argtypes = [P, C.c_int32, P, P, P, P, P]
     lib.madi_grid_build.argtypes = [P, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
                                     P, P, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
-    for name in ("madi_classify", "madi_walk", "madi_reduce_Y", "madi_match",
+    for name in ("madi_classify", "madi_walk", "madi_walk_noalloc", "madi_reduce_Y", "madi_match",
                  "madi_kdtree_build", "madi_grid_build"):
         getattr(lib, name).restype = C.c_int
 

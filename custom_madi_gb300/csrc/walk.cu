@@ -705,3 +705,61 @@ extern "C" madi_status madi_reduce_Y(const double* Y, int64_t n_walkers, int32_t
     if (e != cudaSuccess) return host::cuda_fail(e, "reduce_Y launch");
     return MADI_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free walk.  The persistent walker needs one zeroed 32-bit tile
+// counter besides its inputs and outputs; this entry point keeps it in a
+// file-scope device array instead of a caller buffer, so the caller allocates
+// nothing for it.  The array is 256 bytes (one word used), lives on every GPU
+// that loads this library until the process exits, and is shared by all calls:
+// each call clears the word on its own stream before walking, and two calls
+// that overlap on the GPU race on it.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+#define MADI_WALK_STATIC_SCRATCH_WORDS 64
+static __device__ __align__(256) uint32_t g_walk_static_scratch[MADI_WALK_STATIC_SCRATCH_WORDS];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+uint32_t* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of the static scratch on the current device.  The first call
+// on a device resolves it with cudaGetSymbolAddress (that device current) and
+// caches it.
+madi_status static_scratch(uint32_t** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return host::cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return host::fail(MADI_ERR_UNSUPPORTED, "device ordinal %d beyond %d", dev, kMaxDevices);
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_walk_static_scratch);
+        if (e != cudaSuccess) return host::cuda_fail(e, "cudaGetSymbolAddress(walk scratch)");
+        g_scratch_addr[dev] = static_cast<uint32_t*>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return MADI_OK;
+}
+}  // namespace
+
+extern "C" madi_status madi_walk_noalloc(const madi_walk_desc* desc, void* stream) {
+    host::clear_error();
+    if (!desc) return host::fail(MADI_ERR_INVALID, "null walk descriptor");
+    const int64_t handed_out = (int64_t)desc->n_tiles + (desc->grid_blocks > 0 ? desc->grid_blocks : 0);
+    if (handed_out >= 0x7FFFFFFFll)
+        return host::fail(MADI_ERR_CAPACITY,
+                          "walk_noalloc: %lld tiles + CTAs exceed the static scratch counter (max %d)",
+                          (long long)handed_out, 0x7FFFFFFF - 1);
+    uint32_t* counter = nullptr;
+    madi_status st = static_scratch(&counter);
+    if (st != MADI_OK) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return host::cuda_fail(e, "cudaMemsetAsync(walk scratch)");
+    madi_walk_desc d = *desc;
+    d.work_counter = counter;
+    return madi_walk(&d, stream);
+}

@@ -190,6 +190,21 @@ typedef struct madi_walk_desc {
 
 madi_status madi_walk(const madi_walk_desc* desc, void* stream);
 
+/* madi_walk without any caller-provided scratch; no counterpart in the reference.
+ * For callers that cannot allocate device memory around a walk: code recording a
+ * CUDA graph by stream capture (a cudaMalloc there breaks the capture), plug-in
+ * hosts that hand the library only their own pre-sized input and output buffers,
+ * and services working from a fixed memory pool with no room left for another
+ * buffer.  Same inputs, outputs and results as madi_walk; desc->work_counter is
+ * ignored.  The one zeroed word the persistent walk needs comes from a 256-byte
+ * static device array that every GPU loading the library holds until the process
+ * exits; each call clears it on its stream, all calls share it, and calls that
+ * overlap on the GPU race on it (order them on one stream or with events).  The
+ * first call on a device resolves the array's address (cudaGetSymbolAddress) and
+ * must come before any stream capture.  Walks whose n_tiles + grid_blocks reach
+ * 2^31 - 1 are rejected (MADI_ERR_CAPACITY).  Calls no cudaMalloc or cudaFree. */
+madi_status madi_walk_noalloc(const madi_walk_desc* desc, void* stream);
+
 /* Shared-memory bytes the fp32 walker needs for a geometry of stage_bytes. */
 int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walkers, int32_t n_grid);
 
