@@ -2,7 +2,11 @@
 // _map_kernel_fixed / _map_kernel_free_s0 (madi/fitters_gpu.py:96-154).
 //
 // FP32 path: exhaustive fp32 scan on the CUDA cores, library streamed through
-// shared memory in chunks, one voxel per thread.
+// shared memory in chunks, one voxel per thread.  Fixed S0 scores the centred
+// pair (m - mu, L_j - mu), mu the library column mean: the uncentred expanded
+// form |L_j|^2 - 2 m.L_j rounds at ~|L|^2 2^-24, coarser than the gap between
+// near-tied entries of a dense library, while the centred form rounds at
+// ~|L - mu|^2 2^-24.
 #include <cstdint>
 #include "madi_device.cuh"
 #include "madi_host.h"
@@ -12,22 +16,24 @@ namespace madi {
 constexpr int MATCH_THREADS = 256;
 constexpr int MATCH_CHUNK = 128;
 
-// fixed S0: score_j = |L_j|^2 - 2 m.L_j ; free S0: score_j = -(m.r)^2/|r|^2 when m.r > 0.
+// fixed S0: score_j = |L_j - mu|^2 - 2 (m - mu).(L_j - mu) = |m - L_j|^2 - |m - mu|^2 ;
+// free S0: score_j = -(m.r)^2/|r|^2 when m.r > 0 (mu unused).
 template <int FMAX, int MODE>
 __global__ void __launch_bounds__(MATCH_THREADS) match_fp32_kernel(const float* __restrict__ meas,
-                                                                   const float* __restrict__ lib, int64_t n_vox,
+                                                                   const float* __restrict__ lib,
+                                                                   const float* __restrict__ mu, int64_t n_vox,
                                                                    int n_lib, int n_feat, int32_t* best_idx,
                                                                    float* best_resid, float* best_s0) {
     __shared__ float sl[MATCH_CHUNK][FMAX];
     __shared__ float sn[MATCH_CHUNK];
+    __shared__ float smu[FMAX];
     const int64_t v = (int64_t)blockIdx.x * MATCH_THREADS + threadIdx.x;
+    if (threadIdx.x < FMAX)
+        smu[threadIdx.x] = (MODE == MADI_MATCH_FIXED_S0 && (int)threadIdx.x < n_feat) ? mu[threadIdx.x] : 0.f;
+    __syncthreads();
     float m[FMAX];
-    float mm = 0.f;
 #pragma unroll
-    for (int f = 0; f < FMAX; ++f) {
-        m[f] = (v < n_vox && f < n_feat) ? meas[v * n_feat + f] : 0.f;
-        mm = fmaf(m[f], m[f], mm);
-    }
+    for (int f = 0; f < FMAX; ++f) m[f] = (v < n_vox && f < n_feat) ? meas[v * n_feat + f] - smu[f] : 0.f;
     float best = 3.0e38f;
     int bj = 0;
     for (int base = 0; base < n_lib; base += MATCH_CHUNK) {
@@ -35,7 +41,7 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_fp32_kernel(const float* 
         __syncthreads();
         for (int t = threadIdx.x; t < MATCH_CHUNK * FMAX; t += MATCH_THREADS) {
             const int e = t / FMAX, f = t - e * FMAX;
-            sl[e][f] = (e < cnt && f < n_feat) ? lib[(int64_t)(base + e) * n_feat + f] : 0.f;
+            sl[e][f] = (e < cnt && f < n_feat) ? lib[(int64_t)(base + e) * n_feat + f] - smu[f] : 0.f;
         }
         __syncthreads();
         if (threadIdx.x < MATCH_CHUNK) {
@@ -59,7 +65,9 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_fp32_kernel(const float* 
         }
     }
     if (v >= n_vox) return;
-    // Residual of the chosen entry from the direct difference (no cancellation).
+    // Residual of the chosen entry from the direct difference of the raw data.
+#pragma unroll
+    for (int f = 0; f < FMAX; ++f) m[f] = f < n_feat ? meas[v * n_feat + f] : 0.f;
     const float* L = lib + (int64_t)bj * n_feat;
     float dot = 0.f, rr = 0.f;
 #pragma unroll
@@ -83,14 +91,14 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_fp32_kernel(const float* 
 }
 
 template <int FMAX>
-static madi_status launch_fp32(const madi_match_desc* d, cudaStream_t s) {
+static madi_status launch_fp32(const madi_match_desc* d, float* mu, cudaStream_t s) {
     const int64_t blocks = (d->n_vox + MATCH_THREADS - 1) / MATCH_THREADS;
     if (d->mode == MADI_MATCH_FIXED_S0)
         match_fp32_kernel<FMAX, MADI_MATCH_FIXED_S0><<<(unsigned)blocks, MATCH_THREADS, 0, s>>>(
-            d->measured, d->lib, d->n_vox, d->n_lib, d->n_feat, d->best_idx, d->best_resid, d->best_s0);
+            d->measured, d->lib, mu, d->n_vox, d->n_lib, d->n_feat, d->best_idx, d->best_resid, d->best_s0);
     else
         match_fp32_kernel<FMAX, MADI_MATCH_FREE_S0><<<(unsigned)blocks, MATCH_THREADS, 0, s>>>(
-            d->measured, d->lib, d->n_vox, d->n_lib, d->n_feat, d->best_idx, d->best_resid, d->best_s0);
+            d->measured, d->lib, nullptr, d->n_vox, d->n_lib, d->n_feat, d->best_idx, d->best_resid, d->best_s0);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return host::cuda_fail(e, "match fp32 launch");
     return MADI_OK;
@@ -102,11 +110,15 @@ using namespace madi;
 
 madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s);
 int64_t madi_match_bf16_scratch(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t topk);
+void madi_match_column_mean(const float* lib, int32_t n_lib, int32_t n_feat, float* mu, cudaStream_t s);
+
+// fp32 needs room for the column means (either mode, so one size fits both).
+static constexpr int64_t FP32_SCRATCH = 256;
 
 extern "C" int64_t madi_match_scratch_bytes(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t precision,
                                             int32_t topk) {
     if (precision == MADI_MATCH_BF16) return madi_match_bf16_scratch(n_vox, n_lib, n_feat, topk);
-    return 0;
+    return FP32_SCRATCH;
 }
 
 extern "C" madi_status madi_match(const madi_match_desc* d, void* stream) {
@@ -121,8 +133,18 @@ extern "C" madi_status madi_match(const madi_match_desc* d, void* stream) {
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (d->precision == MADI_MATCH_BF16) return madi_match_bf16(d, s);
     if (d->precision != MADI_MATCH_FP32) return host::fail(MADI_ERR_INVALID, "match: unknown precision");
-    if (d->n_feat <= 8) return launch_fp32<8>(d, s);
-    if (d->n_feat <= 16) return launch_fp32<16>(d, s);
-    if (d->n_feat <= 24) return launch_fp32<24>(d, s);
-    return launch_fp32<32>(d, s);
+    float* mu = nullptr;
+    if (d->mode == MADI_MATCH_FIXED_S0) {
+        if (!d->scratch || d->scratch_bytes < FP32_SCRATCH)
+            return host::fail(MADI_ERR_CAPACITY, "match fp32: scratch %lld < %lld bytes", (long long)d->scratch_bytes,
+                              (long long)FP32_SCRATCH);
+        if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) != 0)
+            return host::fail(MADI_ERR_INVALID, "match fp32: scratch must be 256-byte aligned");
+        mu = static_cast<float*>(d->scratch);
+        madi_match_column_mean(d->lib, d->n_lib, d->n_feat, mu, s);
+    }
+    if (d->n_feat <= 8) return launch_fp32<8>(d, mu, s);
+    if (d->n_feat <= 16) return launch_fp32<16>(d, mu, s);
+    if (d->n_feat <= 24) return launch_fp32<24>(d, mu, s);
+    return launch_fp32<32>(d, mu, s);
 }

@@ -42,29 +42,43 @@ def match_device(measured, lib_mat, *, free_s0: bool = False, precision: str = "
         raise ValueError("measured (n_vox, F) and library (n_lib, F) must share F")
     n_vox, F = M.shape
     prec = {"fp32": N.MADI_MATCH_FP32, "bf16": N.MADI_MATCH_BF16}[precision]
-    idx = torch.empty(n_vox, dtype=torch.int32, device=M.device)
+    # BF16 CTAs that give up on a bounded wait leave their rows at -1
+    idx = (torch.full((n_vox,), -1, dtype=torch.int32, device=M.device) if prec == N.MADI_MATCH_BF16
+           else torch.empty(n_vox, dtype=torch.int32, device=M.device))
     res = torch.empty(n_vox, dtype=torch.float32, device=M.device)
     s0 = torch.empty(n_vox, dtype=torch.float32, device=M.device) if free_s0 else None
     need = int(N.lib().madi_match_scratch_bytes(n_vox, Lm.shape[0], F, prec, int(topk)))
     if need > 0 and (scratch is None or scratch.numel() < need):
-        scratch = torch.empty(need, dtype=torch.uint8, device=M.device)
+        scratch = torch.empty(need + 256, dtype=torch.uint8, device=M.device)
     d = N.MadiMatchDesc()
     d.measured, d.lib, d.n_vox, d.n_lib, d.n_feat = N.ptr(M), N.ptr(Lm), n_vox, Lm.shape[0], F
     d.mode = N.MADI_MATCH_FREE_S0 if free_s0 else N.MADI_MATCH_FIXED_S0
     d.precision, d.topk = prec, int(topk)
     d.best_idx, d.best_resid, d.best_s0 = N.ptr(idx), N.ptr(res), N.ptr(s0)
-    d.scratch, d.scratch_bytes = (N.ptr(scratch), int(scratch.numel())) if need > 0 else (0, 0)
+    if need > 0:
+        base = N.ptr(scratch)
+        pad = (-base) % 256
+        d.scratch, d.scratch_bytes = base + pad, int(scratch.numel()) - pad
+    else:
+        d.scratch, d.scratch_bytes = 0, 0
     s = stream if stream is not None else torch.cuda.current_stream(M.device)
     st = N.lib().madi_match(C.byref(d), s.cuda_stream)
     N.check(st, "madi_match")
     return idx, res, s0
 
 
+def _indices(idx) -> np.ndarray:
+    b = idx.cpu().numpy().astype(np.int64)
+    if np.any(b < 0):
+        raise RuntimeError("tensor-core library match gave up on a bounded wait; no result for some voxels")
+    return b
+
+
 def map_match_gpu(measured_batch, lib_mat, kios_arr, rhos_arr, Vs_arr, *, precision: str = "fp32",
                   topk: int = DEFAULT_TOPK):
     """Fixed-S0 MAP: (kio, rho, V, resid) of the best library entry per voxel."""
     idx, res, _ = match_device(measured_batch, lib_mat, precision=precision, topk=topk)
-    b = idx.cpu().numpy().astype(np.int64)
+    b = _indices(idx)
     return (np.asarray(kios_arr)[b], np.asarray(rhos_arr)[b], np.asarray(Vs_arr)[b],
             res.cpu().numpy().astype(np.float64))
 
@@ -73,6 +87,6 @@ def map_match_fits0_gpu(raw_signal, lib_mat, kios_arr, rhos_arr, Vs_arr, *, prec
                         topk: int = DEFAULT_TOPK):
     """Free-S0 MAP: (kio, rho, V, resid, s0) of the best library entry per voxel."""
     idx, res, s0 = match_device(raw_signal, lib_mat, free_s0=True, precision=precision, topk=topk)
-    b = idx.cpu().numpy().astype(np.int64)
+    b = _indices(idx)
     return (np.asarray(kios_arr)[b], np.asarray(rhos_arr)[b], np.asarray(Vs_arr)[b],
             res.cpu().numpy().astype(np.float64), s0.cpu().numpy().astype(np.float64))

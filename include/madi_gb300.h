@@ -235,12 +235,14 @@ enum { MADI_MATCH_FP32 = 0, MADI_MATCH_BF16 = 1 };
  *   fixed S0: best = argmin_j (|L_j|^2 - 2 m.L_j), resid = |m|^2 + that
  *   free  S0: best = argmin_j over m.L_j > 0 of |m|^2 - (m.L_j)^2/|L_j|^2
  * Ties pick the lowest library index.
- * FP32: exhaustive fp32 scan on the CUDA cores.
- * BF16: tcgen05 BF16 x BF16 -> FP32 (TMEM) scores, a per-voxel top-k (k <= 32)
- *       candidate list, then an fp32 rescore of the k candidates.
+ * FP32: exhaustive fp32 scan on the CUDA cores; fixed S0 scores the pair
+ *       centred on the library column mean (same argmin, ~|L|^2/|L-mu|^2
+ *       smaller rounding than the uncentred form).
+ * BF16: tcgen05 BF16 x BF16 -> FP32 (TMEM) scores, a per-voxel top-k (k of 8,
+ *       16, 32) candidate list, then an fp32 rescore of the k candidates.
  * measured: device fp32 [n_vox][n_feat]; lib: device fp32 [n_lib][n_feat].
- * scratch: device buffer of madi_match_scratch_bytes(...) bytes (contents need
- * no initialisation).
+ * scratch: 256-byte aligned device buffer of madi_match_scratch_bytes(...)
+ * bytes (contents need no initialisation; FP32 free S0 ignores it).
  */
 typedef struct madi_match_desc {
     const float* measured;
