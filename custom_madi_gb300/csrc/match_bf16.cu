@@ -2,23 +2,31 @@
 // voxel fp64 scan of _map_kernel_fixed / _map_kernel_free_s0
 // (madi/fitters_gpu.py:96-154).
 //
-// Per CTA (128 threads, one per voxel row = one TMEM lane; two CTAs per SM)
-// and voxel tile of 128: the voxels are converted to BF16 in shared memory
-// (K = features padded to 32, K-major, no-swizzle UMMA layout); the library,
-// pre-packed once into 8 KB tiles of 128 entries in the same layout, streams
-// through three shared stages by cp.async.bulk; one thread issues tcgen05.mma
-// (M=128, N=128, K=16, two per tile) into one of two 128-column FP32 TMEM
-// accumulators, so the MMA of tile t overlaps the epilogue of tile t-1.  The
-// epilogue reads the scores with tcgen05.ld; scores under the thread's current
-// k-th best are appended to a shared buffer, which the warp folds into a sorted
-// register top-k with bitonic networks when any lane's buffer fills.  The k
-// candidates are rescored in fp32 from the fp32 data and the best (lowest
-// index on ties) is written.
+// One CTA per SM, persistent over voxel tiles of 128 rows.  The voxels of a
+// tile are converted to BF16 in shared memory (K = features padded to 32,
+// K-major, no-swizzle UMMA layout); the library, pre-packed once into 8 KB
+// tiles of 128 entries in the same layout, streams through four shared stages
+// by cp.async.bulk.  Lane 0 of the producer warp issues tcgen05.mma (M=128,
+// N=128, K=16, two per tile) into one of four 128-column FP32 TMEM
+// accumulators.  Two epilogue warpgroups split each tile's columns: every
+// thread owns one voxel row (its TMEM lane) and keeps a top-k of that row over
+// its half of the library.
 //
+// Scores (smaller is better):
 //   fixed S0: score_j = |L~_j|^2 - 2 m~.L~_j  (= |m~ - L~_j|^2 - |m~|^2)
 //   free  S0: score_j = -(m.r~_j)^2 / |r~_j|^2 when m.r~_j > 0
 // with m~ = bf16(m - mu), L~_j = bf16(L_j - mu) (mu the library column mean:
-// centring keeps the BF16 products small) and r~_j = bf16(r_j).
+// centring keeps the BF16 products small) and r~_j = bf16(r_j).  For fixed S0
+// with F <= 29 the bias is folded into the MMA: three extra K columns carry
+// 1 in A and a three-term BF16 split of -|L~_j|^2 / 2 in B, so the accumulator
+// is t_j = m~.L~_j - |L~_j|^2 / 2 = -score_j / 2 to fp32 accuracy.
+//
+// Epilogue per 32-column chunk: the row's 32 keys are staged in shared memory,
+// a 32-bit mask marks those under the row's current k-th best, and only the
+// marked ones are appended to the row's candidate buffer.  When any lane's
+// buffer would overflow, the warp folds all buffers into the sorted register
+// top-k with bitonic networks.  Each warpgroup rescores its k candidates in
+// fp32 from the fp32 data; the two results are combined (lowest index on ties).
 #include <cstdint>
 #include <cuda_bf16.h>
 #include "madi_device.cuh"
@@ -29,18 +37,26 @@ namespace bf16m {
 
 constexpr int TILE_M = 128;                     // voxels per tile (MMA M, TMEM lanes)
 constexpr int TILE_N = 128;                     // library entries per tile (MMA N)
-constexpr int KPAD = 32;                        // features padded to 32 (two K=16 MMAs)
+constexpr int KPAD = 32;                        // features (+ bias columns) padded to 32
+constexpr int BIAS_COLS = 3;                    // folded -|L~|^2/2 as hi + mid + lo BF16
 constexpr int CORE = 128;                       // bytes of one 8x8 BF16 core matrix
 constexpr int SBO = (KPAD / 8) * CORE;          // 512 B between 8-row groups
 constexpr int LBO = CORE;                       // 128 B between K-adjacent core matrices
 constexpr int A_BYTES = TILE_M * KPAD * 2;      // 8 KB
 constexpr int B_BYTES = TILE_N * KPAD * 2;      // 8 KB
-constexpr int AUX_BYTES = TILE_N * 4;           // per-entry |L~|^2 (fixed) or 1/|r~|^2 (free)
-constexpr int STAGES = 3;                       // library tiles in flight
-constexpr int ACCS = 2;                         // TMEM accumulators (MMA t || epilogue t-1)
-constexpr int TMEM_COLS = ACCS * TILE_N;        // 256: two CTAs share an SM's 512 columns
+constexpr int AUX_BYTES = TILE_N * 4;           // per-entry |L~|^2 (aux mode) or 1/|r~|^2 (free)
+constexpr int STAGES = 4;                       // library tiles in flight
+constexpr int ACCS = 4;                         // TMEM accumulators
+constexpr int TMEM_COLS = ACCS * TILE_N;        // 512: the whole TMEM of the SM
+constexpr int EPI_WG = 2;                       // epilogue warpgroups (column halves)
+constexpr int EPI_THREADS = EPI_WG * TILE_M;    // 256
+constexpr int EPI_WARPS = EPI_THREADS / 32;     // 8
+constexpr int THREADS = EPI_THREADS + 32;       // + producer warp
+constexpr int WG_COLS = TILE_N / EPI_WG;        // 64 columns per warpgroup and tile
 constexpr int CAP = 64;                         // per-thread candidate buffer entries
 constexpr uint32_t SPIN_LIMIT = 1u << 22;       // bounded waits (~0.1-1 s)
+
+enum { MODE_FOLD = 0, MODE_AUX = 1, MODE_FREE = 2 };
 
 // Byte offset of element (row, k) in the no-swizzle K-major canonical layout.
 __host__ __device__ __forceinline__ uint32_t canon_off(int row, int k) {
@@ -59,7 +75,7 @@ MADI_DEV uint64_t make_sdesc(uint32_t saddr) {
     return d;                                   // base offset 0, layout type 0 = no swizzle
 }
 
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N = 256, M = 128.
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N = 128, M = 128.
 MADI_DEV uint32_t make_idesc() {
     uint32_t d = 0;
     d |= 1u << 4;                               // D format F32
@@ -76,6 +92,10 @@ MADI_DEV void mbar_init(uint64_t* bar, uint32_t count) {
 
 MADI_DEV void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+MADI_DEV void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(bar)) : "memory");
 }
 
 // Bounded parity wait; returns false after SPIN_LIMIT polls.
@@ -142,30 +162,44 @@ __global__ void column_mean_kernel(const float* lib, int n_lib, int F, float* mu
     if (threadIdx.x == 0) mu[f] = (float)(s[0] / n_lib);
 }
 
-__global__ void pack_library_kernel(const float* lib, int n_lib, int F, int n_tiles, int free_s0, const float* mu,
+__global__ void pack_library_kernel(const float* lib, int n_lib, int F, int n_tiles, int mode, const float* mu,
                                     unsigned char* tiles, float* aux) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (int64_t)n_tiles * TILE_N) return;
     const int t = (int)(e / TILE_N), n = (int)(e % TILE_N);
     unsigned char* tile = tiles + (size_t)t * B_BYTES;
-    float q = 0.f;
+    const bool live = e < n_lib;
+    double q = 0.0;
     for (int k = 0; k < KPAD; ++k) {
         float x = 0.f;
-        if (e < n_lib && k < F) {
+        if (live && k < F) {
             const float v = lib[e * F + k];
-            x = free_s0 ? v : v - mu[k];
+            x = mode == MODE_FREE ? v : v - mu[k];
         }
         const __nv_bfloat16 xb = __float2bfloat16_rn(x);
-        const float xr = __bfloat162float(xb);
-        q = fmaf(xr, xr, q);
+        const double xr = (double)__bfloat162float(xb);
+        q += xr * xr;
         *reinterpret_cast<__nv_bfloat16*>(tile + canon_off(n, k)) = xb;
     }
     // The norm is taken of the ROUNDED entry, so the fixed-S0 score is exactly
     // |m~ - L~|^2 - |m~|^2 of the rounded vectors: its error then scales with the
     // residual |m - L| rather than with |m - mu| |L - mu|, and near-ties keep
     // their order (free S0 likewise scores the rounded pair, through 1/|r~|^2).
-    // Padding entries carry NaN: their score fails every "<" test.
-    aux[e] = e < n_lib ? (free_s0 ? 1.f / fmaxf(q, 1e-30f) : q) : __int_as_float(0x7fc00000);
+    if (mode == MODE_FOLD) {
+        // -q/2 = hi + mid + lo, each BF16, residual ~2^-25 |q|; padding gets -inf
+        const double x = -0.5 * q;
+        const __nv_bfloat16 hi = live ? __float2bfloat16_rn((float)x) : __float2bfloat16_rn(-INFINITY);
+        const double r1 = live ? x - (double)__bfloat162float(hi) : 0.0;
+        const __nv_bfloat16 mid = __float2bfloat16_rn((float)r1);
+        const double r2 = r1 - (double)__bfloat162float(mid);
+        const __nv_bfloat16 lo = __float2bfloat16_rn((float)r2);
+        *reinterpret_cast<__nv_bfloat16*>(tile + canon_off(n, F)) = hi;
+        *reinterpret_cast<__nv_bfloat16*>(tile + canon_off(n, F + 1)) = mid;
+        *reinterpret_cast<__nv_bfloat16*>(tile + canon_off(n, F + 2)) = lo;
+    }
+    // Padding entries carry NaN in aux: their score fails every "<" test.
+    const float qf = (float)q;
+    aux[e] = live ? (mode == MODE_FREE ? 1.f / fmaxf(qf, 1e-30f) : qf) : __int_as_float(0x7fc00000);
 }
 
 // ---------------------------------------------------------------------------
@@ -174,7 +208,7 @@ __global__ void pack_library_kernel(const float* lib, int n_lib, int F, int n_ti
 // no divergence inside the merge).
 // ---------------------------------------------------------------------------
 template <int K>
-MADI_DEV void cswap(float (&a)[K], int (&ai)[K], int i, int l) {   // ascending at (i, l), i < l
+MADI_DEV void cswap(float (&a)[K], int (&ai)[K], int i, int l) {   // ascending at (i, l)
     const bool sw = a[l] < a[i];
     const float x = a[i], y = a[l];
     const int xi = ai[i], yi = ai[l];
@@ -213,8 +247,8 @@ MADI_DEV void bitonic_clean(float (&a)[K], int (&ai)[K]) {
 }
 
 // Folds this thread's buffered (score, index) entries into ks/kj (ascending)
-// K at a time; every lane of the warp takes part.  Buffer entry e of thread
-// tid lives at buf[e * TILE_M].
+// K at a time; every lane of the warp takes part.  Buffer entry e of the
+// thread lives at buf[e * EPI_THREADS].
 template <int K>
 MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, const float2* buf) {
     const int cmax = __reduce_max_sync(0xffffffffu, cnt);
@@ -225,7 +259,7 @@ MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, c
 #pragma unroll
         for (int i = 0; i < K; ++i) {
             float2 e = make_float2(3.0e38f, 0.f);
-            if (base + i < cnt) e = buf[(base + i) * TILE_M];
+            if (base + i < cnt) e = buf[(base + i) * EPI_THREADS];
             b[i] = e.x;
             bj[i] = __float_as_int(e.y);
         }
@@ -243,33 +277,169 @@ MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, c
 }
 
 // ---------------------------------------------------------------------------
-// Main kernel.
+// Main kernel: warps 0-7 are the epilogue (warpgroup h = warp / 4 takes
+// columns [64h, 64h + 64) of every tile; thread tid % 128 = voxel row = TMEM
+// lane), lane 0 of warp 8 is the producer (library loads and MMA issue).
+// Hand-offs use mbarriers only (every wait bounded):
+//   full[s]  / empty[s] : library stage s loaded / consumed by its MMA
+//   accf[a]             : accumulator a holds tile scores (and, in the aux and
+//                         free modes, the tile's aux row has landed)
+//   acce[a]             : the eight epilogue warps are done with accumulator a
+//   afull               : the voxel tile (A operand) is written (warpgroup 0)
+//   lfull               : warpgroup 1's rescored best per row is written
+// Tile sequence g runs over (voxel tile of this CTA, library tile); stage
+// g % STAGES, accumulator g % ACCS.  The k-th completion of a barrier is
+// waited with parity k & 1.
 // ---------------------------------------------------------------------------
 struct Smem {
     unsigned char a[A_BYTES];
     unsigned char b[STAGES][B_BYTES];
-    float aux[STAGES][TILE_N];
-    float2 buf[CAP][TILE_M];
-    uint64_t bar_load[STAGES];
-    uint64_t bar_mma[ACCS];
+    float aux[ACCS][TILE_N];
+    float4 stage[8][EPI_THREADS];       // the 32 keys of the current chunk, 4 per slot
+    float2 buf[CAP][EPI_THREADS];       // candidate buffers (score, index)
+    float4 res1[2][TILE_M];             // warpgroup 1 -> 0: (resid, index, s0, -) per row
+    uint64_t full[STAGES];
+    uint64_t empty[STAGES];
+    uint64_t accf[ACCS];
+    uint64_t acce[ACCS];
+    uint64_t afull;
+    uint64_t lfull;
+    uint64_t drain;
     uint32_t tmem_base;
     int err;
 };
 
+MADI_DEV int err_flag_read(const Smem& S) { return *reinterpret_cast<const volatile int*>(&S.err); }
+
+// Voxel tile -> BF16 canonical A rows (warpgroup 0, each thread its own row),
+// then hand the tile to the async proxy and signal the producer.
+template <int MODE>
+MADI_DEV void write_voxel_tile(Smem& S, const float* __restrict__ meas, const float* __restrict__ mu, int64_t n_vox,
+                               int F, int64_t vt, int r, int lane) {
+    const int64_t row = vt * TILE_M + r;
+    const bool live = row < n_vox;
+    for (int kc = 0; kc < KPAD / 8; ++kc) {
+        __align__(16) __nv_bfloat16 v8[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int k = kc * 8 + i;
+            float x = 0.f;
+            if (live && k < F) x = meas[row * F + k] - (MODE == MODE_FREE ? 0.f : __ldg(mu + k));
+            if (MODE == MODE_FOLD && k >= F && k < F + BIAS_COLS) x = 1.f;
+            v8[i] = __float2bfloat16_rn(x);
+        }
+        *reinterpret_cast<uint4*>(S.a + canon_off(r, kc * 8)) = *reinterpret_cast<const uint4*>(v8);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic -> async proxy
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&S.afull);
+}
+
+template <int MODE>
+MADI_DEV void producer(Smem& S, const unsigned char* __restrict__ tiles, const float* __restrict__ aux, int n_tiles,
+                       int64_t total, uint32_t tmem) {
+    const uint32_t idesc = make_idesc();
+    const uint32_t a_base = smem_u32(S.a);
+    int64_t gl = 0;                                  // library loads issued
+    bool ok = true;
+    auto load = [&](int64_t g) -> bool {
+        const int st = (int)(g % STAGES);
+        if (g >= STAGES && !mbar_wait(&S.empty[st], (uint32_t)((g / STAGES - 1) & 1))) return false;
+        mbar_expect_tx(&S.full[st], B_BYTES);
+        bulk_g2s(S.b[st], tiles + (size_t)(g % n_tiles) * B_BYTES, B_BYTES, &S.full[st]);
+        return true;
+    };
+    for (; gl < total && gl < STAGES; ++gl)
+        if (!load(gl)) { ok = false; break; }
+    for (int64_t g = 0; g < total && ok; ++g) {
+        const int st = (int)(g % STAGES), acc = (int)(g % ACCS);
+        const int tile = (int)(g % n_tiles);
+        if (tile == 0 && !mbar_wait(&S.afull, (uint32_t)((g / n_tiles) & 1))) { ok = false; break; }
+        if (!mbar_wait(&S.full[st], (uint32_t)((g / STAGES) & 1))) { ok = false; break; }
+        if (g >= ACCS && !mbar_wait(&S.acce[acc], (uint32_t)((g / ACCS - 1) & 1))) { ok = false; break; }
+        fence_after();
+        if (MODE != MODE_FOLD) {
+            // the tile's aux row rides on accf[acc] (arrive + tx); the MMA commit is its second arrival
+            mbar_expect_tx(&S.accf[acc], AUX_BYTES);
+            bulk_g2s(S.aux[acc], aux + (size_t)tile * TILE_N, AUX_BYTES, &S.accf[acc]);
+        }
+        const uint32_t b_base = smem_u32(S.b[st]);
+        const uint32_t d = tmem + (uint32_t)(acc * TILE_N);
+        mma_bf16(d, make_sdesc(a_base), make_sdesc(b_base), idesc, 0u);
+        mma_bf16(d, make_sdesc(a_base + 2 * LBO), make_sdesc(b_base + 2 * LBO), idesc, 1u);
+        mma_commit(&S.empty[st]);
+        mma_commit(&S.accf[acc]);
+        // refill the stage MMA g-1 used (stays STAGES-1 tiles ahead without
+        // waiting on the MMA just issued)
+        if (gl < total && gl <= g + STAGES - 1) {
+            if (!load(gl)) { ok = false; break; }
+            ++gl;
+        }
+    }
+    if (!ok) {
+        S.err = 1;
+        // let issued copies and MMAs land before TMEM / shared memory go away
+        for (int st = 0; st < STAGES; ++st) {
+            const int64_t last = gl - 1 - ((gl - 1 - st) % STAGES + STAGES) % STAGES;   // last load into st
+            if (last >= 0) mbar_wait(&S.full[st], (uint32_t)((last / STAGES) & 1));
+        }
+        mma_commit(&S.drain);      // arrives once every earlier MMA is done
+        mbar_wait(&S.drain, 0);
+    }
+}
+
+// fp32 rescore of this thread's k candidates (staged in its buffer) against
+// the fp32 data; lowest index on ties.
 template <int K, bool FREE>
-__global__ void __launch_bounds__(128, 2) match_bf16_kernel(const float* __restrict__ meas, const float* __restrict__ lib,
-                                                            int64_t n_vox, int n_lib, int F,
-                                                            const unsigned char* __restrict__ tiles,
-                                                            const float* __restrict__ aux, const float* __restrict__ mu,
-                                                            int n_tiles, int32_t* best_idx, float* best_resid,
-                                                            float* best_s0, int* err_flag) {
-    static_assert(CAP % K == 0 && CAP >= 64, "buffer holds whole merge batches and a 32-column chunk");
+MADI_DEV void rescore(const float* __restrict__ meas, const float* __restrict__ lib, int64_t row, int n_lib, int F,
+                      const float2* mybuf, float& best, int& bj, float& bs0) {
+    float m[KPAD];
+#pragma unroll
+    for (int k = 0; k < KPAD; ++k) m[k] = k < F ? meas[row * F + k] : 0.f;
+#pragma unroll 4
+    for (int i = 0; i < K; ++i) {
+        const float2 cand = mybuf[i * EPI_THREADS];
+        const int j = __float_as_int(cand.y);
+        if (!(cand.x < 3.0e38f) || j < 0 || j >= n_lib) continue;
+        const float* L = lib + (size_t)j * F;
+        float lv[KPAD];
+#pragma unroll
+        for (int k = 0; k < KPAD; ++k) lv[k] = k < F ? __ldg(L + k) : 0.f;
+        float dot = 0.f, rr = 0.f;
+#pragma unroll
+        for (int k = 0; k < KPAD; ++k)
+            if (k < F) { dot = fmaf(m[k], lv[k], dot); rr = fmaf(lv[k], lv[k], rr); }
+        const float s0 = FREE ? dot / fmaxf(rr, 1e-30f) : 1.f;
+        float res = 0.f;
+#pragma unroll
+        for (int k = 0; k < KPAD; ++k)
+            if (k < F) { const float r = m[k] - s0 * lv[k]; res = fmaf(r, r, res); }
+        if (FREE && !(dot > 0.f)) res = 3.0e38f;
+        if (res < best || (res == best && j < bj)) { best = res; bj = j; bs0 = s0; }
+    }
+}
+
+template <int K, int MODE>
+__global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const float* __restrict__ meas, const float* __restrict__ lib,
+                                                                int64_t n_vox, int n_lib, int F,
+                                                                const unsigned char* __restrict__ tiles,
+                                                                const float* __restrict__ aux, const float* __restrict__ mu,
+                                                                int n_tiles, int32_t* best_idx, float* best_resid,
+                                                                float* best_s0, int* err_flag) {
+    static_assert(CAP % K == 0 && CAP >= 32, "buffer holds whole merge batches and a 32-column chunk");
+    constexpr bool FREE = MODE == MODE_FREE;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
-        for (int i = 0; i < STAGES; ++i) mbar_init(&S.bar_load[i], 1);
-        for (int i = 0; i < ACCS; ++i) mbar_init(&S.bar_mma[i], 1);
+        for (int i = 0; i < STAGES; ++i) { mbar_init(&S.full[i], 1); mbar_init(&S.empty[i], 1); }
+        for (int i = 0; i < ACCS; ++i) {
+            mbar_init(&S.accf[i], MODE == MODE_FOLD ? 1 : 2);
+            mbar_init(&S.acce[i], EPI_WARPS);
+        }
+        mbar_init(&S.afull, 4);
+        mbar_init(&S.lfull, 4);
+        mbar_init(&S.drain, 1);
         S.err = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -282,152 +452,117 @@ __global__ void __launch_bounds__(128, 2) match_bf16_kernel(const float* __restr
     __syncthreads();
     fence_after();
     const uint32_t tmem = S.tmem_base;
-    const uint32_t idesc = make_idesc();
-    // mbarrier phase bits and thread 0's in-flight async work (drained on
-    // error), one bit per stage / accumulator so they stay in registers
-    uint32_t ph_load = 0, ph_mma = 0, load_busy = 0, mma_busy = 0;
     const int64_t n_vtiles = (n_vox + TILE_M - 1) / TILE_M;
-    const float2* mybuf = &S.buf[0][tid];
-    float2* mybuf_w = &S.buf[0][tid];
-    const uint32_t a_base = smem_u32(S.a);
-    bool ok = true;
+    const int64_t my_vt = (int64_t)blockIdx.x < n_vtiles ? (n_vtiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
-    for (int64_t vt = blockIdx.x; vt < n_vtiles && ok; vt += gridDim.x) {
-        // ---- prologue loads: the stages are free (previous tile fully drained) ----
-        if (tid == 0) {
-            for (int s = 0; s < STAGES && s < n_tiles; ++s) {
-                mbar_expect_tx(&S.bar_load[s], B_BYTES + AUX_BYTES);
-                bulk_g2s(S.b[s], tiles + (size_t)s * B_BYTES, B_BYTES, &S.bar_load[s]);
-                bulk_g2s(S.aux[s], aux + (size_t)s * TILE_N, AUX_BYTES, &S.bar_load[s]);
-                load_busy |= 1u << s;
-            }
-        }
-        const int64_t row = vt * TILE_M + tid;
-        const bool live = row < n_vox;
-        // ---- voxel tile -> BF16 canonical A (each thread its own row) ----
-        for (int kc = 0; kc < KPAD / 8; ++kc) {
-            __align__(16) __nv_bfloat16 v8[8];
+    if (warp == EPI_WARPS) {
+        if (lane == 0) producer<MODE>(S, tiles, aux, n_tiles, my_vt * n_tiles, tmem);
+    } else {
+        const int wg = warp >> 2;                    // column half
+        const int r = tid & (TILE_M - 1);            // voxel row = TMEM lane
+        const float2* mybuf = &S.buf[0][tid];
+        float2* mybuf_w = &S.buf[0][tid];
+        float4* mystage = &S.stage[0][tid];
+        const float* mystage_f = reinterpret_cast<const float*>(mystage);
+        int64_t g = 0;
+        bool ok = true;
+        if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, meas, mu, n_vox, F, blockIdx.x, r, lane);
+        for (int64_t lv = 0; lv < my_vt && ok; ++lv) {
+            const int64_t vt = blockIdx.x + lv * gridDim.x;
+            float ks[K];
+            int kj[K];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int k = kc * 8 + i;
-                float x = 0.f;
-                if (live && k < F) x = meas[row * F + k] - (FREE ? 0.f : __ldg(mu + k));
-                v8[i] = __float2bfloat16_rn(x);
-            }
-            *reinterpret_cast<uint4*>(S.a + canon_off(tid, kc * 8)) = *reinterpret_cast<const uint4*>(v8);
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic -> async proxy (A tile)
-        __syncthreads();
-        float ks[K];
-        int kj[K];
-#pragma unroll
-        for (int i = 0; i < K; ++i) { ks[i] = 3.0e38f; kj[i] = 0; }
-        float thr = 3.0e38f;
-        int cnt = 0;
-        for (int t = 0; t <= n_tiles && ok; ++t) {
-            // ---- issue the MMA of tile t into accumulator t & 1 ----
-            if (t < n_tiles && tid == 0) {
-                const int st = t % STAGES;
-                if (mbar_wait(&S.bar_load[st], (ph_load >> st) & 1u)) {
-                    load_busy &= ~(1u << st);
-                    ph_load ^= 1u << st;
-                } else {
-                    S.err = 1;
-                }
-                if (!S.err) {
-                    fence_after();
-                    const uint32_t b_base = smem_u32(S.b[st]);
-                    const uint32_t d = tmem + (uint32_t)((t & 1) * TILE_N);
-                    mma_bf16(d, make_sdesc(a_base), make_sdesc(b_base), idesc, 0u);
-                    mma_bf16(d, make_sdesc(a_base + 2 * LBO), make_sdesc(b_base + 2 * LBO), idesc, 1u);
-                    mma_commit(&S.bar_mma[t & 1]);
-                    mma_busy |= 1u << (t & 1);
-                }
-            }
-            if (t == 0) continue;
-            // ---- epilogue of tile t-1 while MMA t runs ----
-            const int tt = t - 1, acc = tt & 1, st = tt % STAGES;
-            if (mbar_wait(&S.bar_mma[acc], (ph_mma >> acc) & 1u)) mma_busy &= ~(1u << acc);
-            else S.err = 1;
-            ph_mma ^= 1u << acc;
-            fence_after();
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(acc * TILE_N);
-            const float* ax = S.aux[st];
-            const int jb = tt * TILE_N;
+            for (int i = 0; i < K; ++i) { ks[i] = 3.0e38f; kj[i] = 0; }
+            float thr = 3.0e38f;
+            float tthr = -1.5e38f;                   // fold mode: key t hits when t > -thr / 2
+            int cnt = 0;
+            for (int t = 0; t < n_tiles; ++t, ++g) {
+                const int acc = (int)(g % ACCS);
+                const bool got_lane = mbar_wait(&S.accf[acc], (uint32_t)((g / ACCS) & 1)) && !err_flag_read(S);
+                const bool got = __all_sync(0xffffffffu, got_lane);   // warp-uniform
+                if (!got) { S.err = 1; ok = false; break; }
+                fence_after();
+                const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(acc * TILE_N + wg * WG_COLS);
+                const float* ax = S.aux[acc] + wg * WG_COLS;
+                const int jb = t * TILE_N + wg * WG_COLS;
 #pragma unroll 1
-            for (int c = 0; c < TILE_N; c += 32) {
-                if (__any_sync(0xffffffffu, cnt > CAP - 32)) merge_buffer<K>(ks, kj, thr, cnt, mybuf);
-                float v[32];
-                tmem_ld32(taddr + (uint32_t)c, v);
-                float q[32];
+                for (int c = 0; c < WG_COLS; c += 32) {
+                    float key[32];
+                    tmem_ld32(taddr + (uint32_t)c, key);
+                    if (MODE != MODE_FOLD) {
 #pragma unroll
-                for (int i = 0; i < 32; i += 4) {
-                    const float4 a4 = *reinterpret_cast<const float4*>(ax + c + i);
-                    q[i] = a4.x; q[i + 1] = a4.y; q[i + 2] = a4.z; q[i + 3] = a4.w;
-                }
+                        for (int i = 0; i < 32; i += 4) {
+                            const float4 q = *reinterpret_cast<const float4*>(ax + c + i);
+                            const float qq[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const float sc = FREE ? (-v[i] * fabsf(v[i])) * q[i] : fmaf(-2.f, v[i], q[i]);
-                    if (sc < thr) {
-                        mybuf_w[cnt * TILE_M] = make_float2(sc, __int_as_float(jb + c + i));
-                        ++cnt;
+                            for (int u = 0; u < 4; ++u) {
+                                const float v = key[i + u];
+                                key[i + u] = FREE ? (-v * fabsf(v)) * qq[u] : fmaf(-2.f, v, qq[u]);
+                            }
+                        }
                     }
+#pragma unroll
+                    for (int i = 0; i < 32; i += 4)
+                        mystage[(i >> 2) * EPI_THREADS] = make_float4(key[i], key[i + 1], key[i + 2], key[i + 3]);
+                    // four independent 8-bit masks, then one 32-bit mask
+                    uint32_t mk[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) {
+                        const bool hit = MODE == MODE_FOLD ? key[i] > tthr : key[i] < thr;
+                        if (hit) mk[i >> 3] |= 1u << (i & 7);
+                    }
+                    uint32_t m = mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24);
+                    const int nh = __popc(m);
+                    if (__any_sync(0xffffffffu, cnt + nh > CAP)) {
+                        merge_buffer<K>(ks, kj, thr, cnt, mybuf);
+                        tthr = -0.5f * thr;
+                    }
+                    float2* wp = mybuf_w + cnt * EPI_THREADS;
+                    const int jc = jb + c;
+                    while (m) {
+                        const int i = __ffs(m) - 1;
+                        m &= m - 1;
+                        const float kv = mystage_f[(i >> 2) * (EPI_THREADS * 4) + (i & 3)];
+                        *wp = make_float2(MODE == MODE_FOLD ? -2.f * kv : kv, __int_as_float(jc + i));
+                        wp += EPI_THREADS;
+                    }
+                    cnt += nh;
                 }
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.acce[acc]);
             }
-            fence_before();
-            __syncthreads();   // accumulator acc and stage st are free again
-            if (tid == 0 && tt + STAGES < n_tiles && !S.err) {
-                mbar_expect_tx(&S.bar_load[st], B_BYTES + AUX_BYTES);
-                bulk_g2s(S.b[st], tiles + (size_t)(tt + STAGES) * B_BYTES, B_BYTES, &S.bar_load[st]);
-                bulk_g2s(S.aux[st], aux + (size_t)(tt + STAGES) * TILE_N, AUX_BYTES, &S.bar_load[st]);
-                load_busy |= 1u << st;
-            }
-            if (S.err) ok = false;
-        }
-        if (!ok) break;
-        merge_buffer<K>(ks, kj, thr, cnt, mybuf);
-        // the (now empty) buffer carries the candidates to the rescore loop, so
-        // ks/kj are only ever indexed by constants and stay in registers
+            if (!ok) break;
+            // every MMA of this voxel tile is complete: the next tile's A may go in now
+            if (wg == 0 && lv + 1 < my_vt) write_voxel_tile<MODE>(S, meas, mu, n_vox, F, vt + gridDim.x, r, lane);
+            merge_buffer<K>(ks, kj, thr, cnt, mybuf);
+            // the (now empty) buffer carries the candidates to the rescore loop, so
+            // ks/kj are only ever indexed by constants and stay in registers
 #pragma unroll
-        for (int i = 0; i < K; ++i) mybuf_w[i * TILE_M] = make_float2(ks[i], __int_as_float(kj[i]));
-        // ---- fp32 rescore of the k candidates from the fp32 data ----
-        if (live) {
-            float m[KPAD];
-#pragma unroll
-            for (int k = 0; k < KPAD; ++k) m[k] = k < F ? meas[row * F + k] : 0.f;
+            for (int i = 0; i < K; ++i) mybuf_w[i * EPI_THREADS] = make_float2(ks[i], __int_as_float(kj[i]));
+            const int64_t row = vt * TILE_M + r;
             float best = 3.0e38f, bs0 = 0.f;
             int bj = 0x7FFFFFFF;
-#pragma unroll 1
-            for (int i = 0; i < K; ++i) {
-                const float2 cand = mybuf[i * TILE_M];
-                const int j = __float_as_int(cand.y);
-                if (!(cand.x < 3.0e38f) || j < 0 || j >= n_lib) continue;
-                const float* L = lib + (size_t)j * F;
-                float dot = 0.f, rr = 0.f;
-#pragma unroll
-                for (int k = 0; k < KPAD; ++k)
-                    if (k < F) { dot = fmaf(m[k], L[k], dot); rr = fmaf(L[k], L[k], rr); }
-                const float s0 = FREE ? dot / fmaxf(rr, 1e-30f) : 1.f;
-                float res = 0.f;
-#pragma unroll
-                for (int k = 0; k < KPAD; ++k)
-                    if (k < F) { const float r = m[k] - s0 * L[k]; res = fmaf(r, r, res); }
-                if (FREE && !(dot > 0.f)) res = 3.0e38f;
-                if (res < best || (res == best && j < bj)) { best = res; bj = j; bs0 = s0; }
+            if (row < n_vox) rescore<K, FREE>(meas, lib, row, n_lib, F, mybuf, best, bj, bs0);
+            if (wg == 1) {
+                S.res1[lv & 1][r] = make_float4(best, __int_as_float(bj), bs0, 0.f);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.lfull);
+            } else {
+                const bool got_lane = mbar_wait(&S.lfull, (uint32_t)(lv & 1));
+                if (!__all_sync(0xffffffffu, got_lane)) { S.err = 1; ok = false; break; }
+                const float4 o = S.res1[lv & 1][r];
+                const int j1 = __float_as_int(o.y);
+                if (o.x < best || (o.x == best && j1 < bj)) { best = o.x; bj = j1; bs0 = o.z; }
+                if (row < n_vox) {
+                    best_idx[row] = bj == 0x7FFFFFFF ? 0 : bj;
+                    best_resid[row] = best;
+                    if (FREE && best_s0) best_s0[row] = bs0;
+                }
             }
-            best_idx[row] = bj == 0x7FFFFFFF ? 0 : bj;
-            best_resid[row] = best;
-            if (FREE && best_s0) best_s0[row] = bs0;
         }
-        __syncthreads();
     }
-    // ---- teardown: no copy or MMA may still be in flight when TMEM is freed ----
-    if (tid == 0 && S.err) {
-        for (int b = 0; b < STAGES; ++b)
-            if ((load_busy >> b) & 1u) mbar_wait(&S.bar_load[b], (ph_load >> b) & 1u);
-        for (int b = 0; b < ACCS; ++b)
-            if ((mma_busy >> b) & 1u) mbar_wait(&S.bar_mma[b], (ph_mma >> b) & 1u);
-    }
+    // ---- teardown: the producer has drained its copies and MMAs on error ----
     fence_before();
     __syncthreads();
     fence_after();
@@ -472,40 +607,38 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     float* mu = reinterpret_cast<float*>(base + round256((int64_t)n_tiles * B_BYTES) + round256((int64_t)n_tiles * TILE_N * 4));
     int* err = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(mu) + round256(KPAD * 4));
     const bool free_s0 = d->mode == MADI_MATCH_FREE_S0;
+    const int mode = free_s0 ? MODE_FREE : (d->n_feat + BIAS_COLS <= KPAD ? MODE_FOLD : MODE_AUX);
     cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), s);
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");
     if (!free_s0) column_mean_kernel<<<d->n_feat, 256, 0, s>>>(d->lib, d->n_lib, d->n_feat, mu);
     const int64_t n_ent = (int64_t)n_tiles * TILE_N;
-    pack_library_kernel<<<(unsigned)((n_ent + 255) / 256), 256, 0, s>>>(d->lib, d->n_lib, d->n_feat, n_tiles,
-                                                                         free_s0 ? 1 : 0, mu, tiles, aux);
+    pack_library_kernel<<<(unsigned)((n_ent + 255) / 256), 256, 0, s>>>(d->lib, d->n_lib, d->n_feat, n_tiles, mode, mu,
+                                                                         tiles, aux);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t n_vtiles = (d->n_vox + TILE_M - 1) / TILE_M;
     const size_t smem = sizeof(Smem);
-#define MADI_LAUNCH_BF16(KK, FR)                                                                          \
+    // one CTA per SM: it allocates all 512 TMEM columns
+    const int grid = (int)std::min<int64_t>(n_vtiles, (int64_t)sms);
+#define MADI_LAUNCH_BF16(KK, MD)                                                                          \
     do {                                                                                                  \
-        auto k = match_bf16_kernel<KK, FR>;                                                               \
+        auto k = match_bf16_kernel<KK, MD>;                                                               \
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);             \
         if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 attribute");                          \
-        int per_sm = 0;                                                                                   \
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, smem);                         \
-        if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 occupancy");                          \
-        /* TMEM: at most 512 / TMEM_COLS CTAs may hold columns on one SM */                               \
-        per_sm = std::max(1, std::min(per_sm, 512 / TMEM_COLS));                                          \
-        const int grid = (int)std::min<int64_t>(n_vtiles, (int64_t)sms * per_sm);                        \
-        k<<<grid, 128, smem, s>>>(d->measured, d->lib, d->n_vox, d->n_lib, d->n_feat, tiles, aux, mu,    \
-                                  n_tiles, d->best_idx, d->best_resid, d->best_s0, err);                 \
+        k<<<grid, THREADS, smem, s>>>(d->measured, d->lib, d->n_vox, d->n_lib, d->n_feat, tiles, aux, mu, \
+                                      n_tiles, d->best_idx, d->best_resid, d->best_s0, err);              \
     } while (0)
-    if (free_s0) {
-        if (d->topk == 8) MADI_LAUNCH_BF16(8, true);
-        else if (d->topk == 16) MADI_LAUNCH_BF16(16, true);
-        else MADI_LAUNCH_BF16(32, true);
-    } else {
-        if (d->topk == 8) MADI_LAUNCH_BF16(8, false);
-        else if (d->topk == 16) MADI_LAUNCH_BF16(16, false);
-        else MADI_LAUNCH_BF16(32, false);
-    }
+#define MADI_LAUNCH_BF16_K(MD)                                                                            \
+    do {                                                                                                  \
+        if (d->topk == 8) MADI_LAUNCH_BF16(8, MD);                                                        \
+        else if (d->topk == 16) MADI_LAUNCH_BF16(16, MD);                                                 \
+        else MADI_LAUNCH_BF16(32, MD);                                                                    \
+    } while (0)
+    if (mode == MODE_FOLD) MADI_LAUNCH_BF16_K(MODE_FOLD);
+    else if (mode == MODE_AUX) MADI_LAUNCH_BF16_K(MODE_AUX);
+    else MADI_LAUNCH_BF16_K(MODE_FREE);
+#undef MADI_LAUNCH_BF16_K
 #undef MADI_LAUNCH_BF16
     e = cudaGetLastError();
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 launch");
