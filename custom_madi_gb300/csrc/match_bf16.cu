@@ -45,7 +45,8 @@ constexpr int LBO = CORE;                       // 128 B between K-adjacent core
 constexpr int A_BYTES = TILE_M * KPAD * 2;      // 8 KB
 constexpr int B_BYTES = TILE_N * KPAD * 2;      // 8 KB
 constexpr int AUX_BYTES = TILE_N * 4;           // per-entry |L~|^2 (aux mode) or 1/|r~|^2 (free)
-constexpr int STAGES = 4;                       // library tiles in flight
+constexpr int STAGES = 8;                       // library tiles in flight
+constexpr int LOAD_AHEAD = 4;                   // library tiles loaded ahead of the MMA
 constexpr int ACCS = 4;                         // TMEM accumulators
 constexpr int TMEM_COLS = ACCS * TILE_N;        // 512: the whole TMEM of the SM
 constexpr int EPI_WG = 2;                       // epilogue warpgroups (column halves)
@@ -53,8 +54,9 @@ constexpr int EPI_THREADS = EPI_WG * TILE_M;    // 256
 constexpr int EPI_WARPS = EPI_THREADS / 32;     // 8
 constexpr int THREADS = EPI_THREADS + 32;       // + producer warp
 constexpr int WG_COLS = TILE_N / EPI_WG;        // 64 columns per warpgroup and tile
-constexpr int CAP = 64;                         // per-thread candidate buffer entries
-constexpr uint32_t SPIN_LIMIT = 1u << 22;       // bounded waits (~0.1-1 s)
+constexpr int CAP = 32;                         // per-thread candidate buffer entries
+constexpr uint32_t SUSPEND_NS = 20000;          // mbarrier try_wait suspend hint
+constexpr uint32_t SPIN_LIMIT = 50000;          // bounded waits: <= SPIN_LIMIT * SUSPEND_NS ~ 1 s
 
 enum { MODE_FOLD = 0, MODE_AUX = 1, MODE_FREE = 2 };
 
@@ -99,12 +101,22 @@ MADI_DEV void mbar_arrive(uint64_t* bar) {
 }
 
 // Bounded parity wait; returns false after SPIN_LIMIT polls.
+MADI_DEV bool mbar_wait(uint64_t* bar, uint32_t parity);
+
+// Warp-wide bounded wait polled by lane 0 only (the other lanes would only add
+// shared-memory traffic); the result is the same on every lane.
+MADI_DEV bool mbar_wait_warp(uint64_t* bar, uint32_t parity, int lane) {
+    bool ok = false;
+    if (lane == 0) ok = mbar_wait(bar, parity);
+    return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+}
+
 MADI_DEV bool mbar_wait(uint64_t* bar, uint32_t parity) {
     const uint32_t a = smem_u32(bar);
     for (uint32_t i = 0; i < SPIN_LIMIT; ++i) {
         uint32_t done;
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                     : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(a), "r"(parity), "r"(SUSPEND_NS) : "memory");
         if (done) return true;
     }
     return false;
@@ -145,6 +157,23 @@ MADI_DEV void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 64 consecutive FP32 columns of this warp's 32 lanes (one load, one wait).
+#define MADI_R8(i) "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), \
+                   "=r"(r[i + 6]), "=r"(r[i + 7])
+MADI_DEV void tmem_ld64(uint32_t taddr, float* v) {
+    uint32_t r[64];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+                 "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+                 "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+                 : MADI_R8(0), MADI_R8(8), MADI_R8(16), MADI_R8(24), MADI_R8(32), MADI_R8(40), MADI_R8(48), MADI_R8(56)
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+#undef MADI_R8
+
 // ---------------------------------------------------------------------------
 // Library packing: fp32 [n_lib][F] -> BF16 canonical tiles, per-entry aux.
 // ---------------------------------------------------------------------------
@@ -162,24 +191,29 @@ __global__ void column_mean_kernel(const float* lib, int n_lib, int F, float* mu
     if (threadIdx.x == 0) mu[f] = (float)(s[0] / n_lib);
 }
 
+// Library entry e of the scan order is row lperm[e] of the caller's library.
+// Also copies the fp32 row into lrows[e][0..KPAD) (zero padded, 128-byte rows)
+// for the rescore.
 __global__ void pack_library_kernel(const float* lib, int n_lib, int F, int n_tiles, int mode, const float* mu,
-                                    unsigned char* tiles, float* aux) {
+                                    const int32_t* lperm, unsigned char* tiles, float* aux, float* lrows) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (int64_t)n_tiles * TILE_N) return;
     const int t = (int)(e / TILE_N), n = (int)(e % TILE_N);
     unsigned char* tile = tiles + (size_t)t * B_BYTES;
     const bool live = e < n_lib;
+    const int64_t src = live ? lperm[e] : 0;
     double q = 0.0;
     for (int k = 0; k < KPAD; ++k) {
         float x = 0.f;
         if (live && k < F) {
-            const float v = lib[e * F + k];
+            const float v = lib[src * F + k];
             x = mode == MODE_FREE ? v : v - mu[k];
         }
         const __nv_bfloat16 xb = __float2bfloat16_rn(x);
         const double xr = (double)__bfloat162float(xb);
         q += xr * xr;
         *reinterpret_cast<__nv_bfloat16*>(tile + canon_off(n, k)) = xb;
+        if (live) lrows[e * KPAD + k] = k < F ? lib[src * F + k] : 0.f;
     }
     // The norm is taken of the ROUNDED entry, so the fixed-S0 score is exactly
     // |m~ - L~|^2 - |m~|^2 of the rounded vectors: its error then scales with the
@@ -200,6 +234,263 @@ __global__ void pack_library_kernel(const float* lib, int n_lib, int F, int n_ti
     // Padding entries carry NaN in aux: their score fails every "<" test.
     const float qf = (float)q;
     aux[e] = live ? (mode == MODE_FREE ? 1.f / fmaxf(qf, 1e-30f) : qf) : __int_as_float(0x7fc00000);
+}
+
+// ---------------------------------------------------------------------------
+// Scan order.  The library is sorted along its principal axis and each voxel
+// tile (voxels bucketed along the same axis) visits the library tiles nearest
+// its key first, so the rows' k-th best thresholds settle within a few tiles
+// and later tiles rarely hold a candidate.  The order changes no result: the
+// top-k of a row is the k smallest scores whatever the visiting order.  Keys
+// are (x - kmu).pc with x the row (free S0: the unit row), kmu the library mean
+// of such rows and pc the leading eigenvector of their covariance.
+// ---------------------------------------------------------------------------
+constexpr int NBUCKET = 256;                    // voxel key buckets
+constexpr int SORT_MAX = 32768;                 // libraries up to this size are sorted
+constexpr int VBLK = 1024;                      // voxels per ranking block
+
+MADI_DEV float row_scale(const float* x, int F, bool unit) {
+    if (!unit) return 1.f;
+    float s = 0.f;
+    for (int k = 0; k < F; ++k) s = fmaf(x[k], x[k], s);
+    return s > 0.f ? rsqrtf(s) : 0.f;
+}
+
+// kmu[f] over rows (fp64 sums, fixed order); one block per column.
+__global__ void key_mean_kernel(const float* lib, int n_lib, int F, int unit, float* kmu) {
+    __shared__ double sh[256];
+    const int f = blockIdx.x;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n_lib; i += blockDim.x) {
+        const float* x = lib + (size_t)i * F;
+        acc += (double)(x[f] * row_scale(x, F, unit != 0));
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) kmu[f] = (float)(sh[0] / n_lib);
+}
+
+// cov[a][b] for a <= b (mirrored), one block per pair.
+__global__ void key_cov_kernel(const float* lib, int n_lib, int F, int unit, const float* kmu, float* cov) {
+    __shared__ double sh[256];
+    const int a = blockIdx.x / F, b = blockIdx.x % F;
+    if (a > b) return;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n_lib; i += blockDim.x) {
+        const float* x = lib + (size_t)i * F;
+        const float sc = row_scale(x, F, unit != 0);
+        acc += (double)(x[a] * sc - kmu[a]) * (double)(x[b] * sc - kmu[b]);
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cov[a * F + b] = cov[b * F + a] = (float)(sh[0] / n_lib);
+}
+
+// Leading eigenvector by power iteration (one warp, fixed start and count).
+__global__ void key_axis_kernel(const float* cov, int F, float* pc) {
+    const int lane = threadIdx.x;
+    float v = lane < F ? 1.f + 0.01f * lane : 0.f;
+    for (int it = 0; it < 200; ++it) {
+        float w = 0.f;
+        for (int b = 0; b < F; ++b) w = fmaf(lane < F ? cov[lane * F + b] : 0.f, __shfl_sync(0xffffffffu, v, b), w);
+        float n2 = w * w;
+        for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+        v = n2 > 0.f ? w * rsqrtf(n2) : v;
+    }
+    if (lane < F) pc[lane] = v;
+}
+
+__global__ void key_kernel(const float* x, int64_t n, int F, int unit, const float* kmu, const float* pc, float* key) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* r = x + i * F;
+    const float sc = row_scale(r, F, unit != 0);
+    float k = 0.f;
+    for (int f = 0; f < F; ++f) k = fmaf(r[f] * sc - kmu[f], pc[f], k);
+    key[i] = k;
+}
+
+// One CTA: library order by quantised key (17 bits) then index (15 bits), a
+// deterministic bitonic sort of packed words in shared memory; also the key
+// range.  n <= SORT_MAX.
+__global__ void __launch_bounds__(1024) lib_sort_kernel(const float* key, int n, int32_t* lperm, float* krange) {
+    extern __shared__ uint32_t w[];
+    __shared__ float red[2][32];
+    int n2 = 1;
+    while (n2 < n) n2 <<= 1;
+    float lo = 3.0e38f, hi = -3.0e38f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { lo = fminf(lo, key[i]); hi = fmaxf(hi, key[i]); }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = lo; red[1][threadIdx.x >> 5] = hi; }
+    __syncthreads();
+    lo = red[0][0]; hi = red[1][0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) { lo = fminf(lo, red[0][i]); hi = fmaxf(hi, red[1][i]); }
+    const float scale = hi > lo ? 131071.f / (hi - lo) : 0.f;
+    for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        if (i < n) {
+            const uint32_t q = (uint32_t)fminf(fmaxf((key[i] - lo) * scale, 0.f), 131071.f);
+            w[i] = (q << 15) | (uint32_t)i;
+        } else {
+            w[i] = 0xFFFFFFFFu;
+        }
+    }
+    __syncthreads();
+    for (int k = 2; k <= n2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint32_t x = w[i], y = w[l];
+                    const bool up = (i & k) == 0;
+                    if ((x > y) == up) { w[i] = y; w[l] = x; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) lperm[i] = (int32_t)(w[i] & 0x7FFFu);
+    if (threadIdx.x == 0) { krange[0] = lo; krange[1] = hi; }
+}
+
+__global__ void iota_kernel(int32_t* p, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = (int32_t)i;
+}
+
+// Key bounds of each library tile in scan order.
+__global__ void tile_bounds_kernel(const float* key, const int32_t* lperm, int n_lib, int n_tiles, float* tlo,
+                                   float* thi) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const int a = t * TILE_N, b = min((t + 1) * TILE_N, n_lib) - 1;
+    tlo[t] = key[lperm[a]];
+    thi[t] = key[lperm[b]];
+}
+
+// Voxel key bucket (over the library key range; outside values clamp).
+__global__ void vox_bucket_kernel(const float* meas, int64_t n_vox, int F, int unit, const float* kmu, const float* pc,
+                                  const float* krange, float* vkey, uint8_t* vb) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_vox) return;
+    const float* r = meas + i * F;
+    const float sc = row_scale(r, F, unit != 0);
+    float k = 0.f;
+    for (int f = 0; f < F; ++f) k = fmaf(r[f] * sc - kmu[f], pc[f], k);
+    vkey[i] = k;
+    const float lo = krange[0], hi = krange[1];
+    const float u = hi > lo ? (k - lo) / (hi - lo) : 0.f;
+    vb[i] = (uint8_t)fminf(fmaxf(u * NBUCKET, 0.f), (float)(NBUCKET - 1));
+}
+
+// Stable rank of each voxel among the earlier voxels of its block with the
+// same bucket (warp match + per-warp histograms), and per-block counts.
+__global__ void __launch_bounds__(VBLK) vox_rank_kernel(const uint8_t* vb, int64_t n_vox, uint16_t* vrank,
+                                                        uint32_t* cnt) {
+    __shared__ uint32_t hw[VBLK / 32][NBUCKET];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < (VBLK / 32) * NBUCKET; i += blockDim.x) (&hw[0][0])[i] = 0u;
+    __syncthreads();
+    const int64_t v = (int64_t)blockIdx.x * VBLK + threadIdx.x;
+    const int b = v < n_vox ? (int)vb[v] : NBUCKET;         // NBUCKET: no voxel
+    const uint32_t same = __match_any_sync(0xffffffffu, b);
+    const uint32_t rank_w = __popc(same & ((1u << lane) - 1u));
+    if (b < NBUCKET && rank_w == 0) hw[warp][b] = __popc(same);
+    __syncthreads();
+    if (threadIdx.x < NBUCKET) {
+        uint32_t run = 0;
+        for (int w = 0; w < VBLK / 32; ++w) { const uint32_t c = hw[w][threadIdx.x]; hw[w][threadIdx.x] = run; run += c; }
+        cnt[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = run;   // bucket-major
+    }
+    __syncthreads();
+    if (b < NBUCKET) vrank[v] = (uint16_t)(hw[warp][b] + rank_w);
+}
+
+// Per bucket (one block each): exclusive prefix of its per-block counts
+// (offs[b][blk]) and the bucket total.
+__global__ void __launch_bounds__(1024) vox_scan_kernel(const uint32_t* cnt, int nblk, uint32_t* offs, uint32_t* tot) {
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
+    const int b = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nblk; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const uint32_t c = i < nblk ? cnt[(size_t)b * nblk + i] : 0u;
+        uint32_t x = c;                                   // inclusive warp scan
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = wsum[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            wsum[lane] = w;                               // inclusive over warps
+        }
+        __syncthreads();
+        const uint32_t before = carry + (warp > 0 ? wsum[warp - 1] : 0u) + x - c;
+        if (i < nblk) offs[(size_t)b * nblk + i] = before;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += wsum[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tot[b] = carry;
+}
+
+// Exclusive scan of the bucket totals (one warp-sized block per 32 buckets, serial).
+__global__ void vox_base_kernel(uint32_t* tot) {
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int i = 0; i < NBUCKET; ++i) { const uint32_t c = tot[i]; tot[i] = run; run += c; }
+    }
+}
+
+__global__ void vox_scatter_kernel(const uint8_t* vb, const uint16_t* vrank, const uint32_t* offs, const uint32_t* base,
+                                   int64_t n_vox, int nblk, int32_t* vperm) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_vox) return;
+    const int64_t blk = v / VBLK;
+    const int b = vb[v];
+    vperm[base[b] + offs[(size_t)b * nblk + blk] + vrank[v]] = (int32_t)v;
+}
+
+// Scan order of the library tiles for each voxel tile: the tile holding the
+// voxel tile's median key first, then outward by key distance.
+__global__ void order_kernel(const float* vkey, const int32_t* vperm, int64_t n_vox, int64_t n_vtiles,
+                             const float* tlo, const float* thi, int n_tiles, int sorted, uint16_t* order) {
+    const int64_t vt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (vt >= n_vtiles) return;
+    uint16_t* o = order + vt * n_tiles;
+    if (!sorted) {
+        for (int s = 0; s < n_tiles; ++s) o[s] = (uint16_t)s;
+        return;
+    }
+    const float key = vkey[vperm[min(vt * TILE_M + TILE_M / 2, n_vox - 1)]];
+    int t0 = 0;
+    while (t0 < n_tiles - 1 && thi[t0] < key) ++t0;
+    o[0] = (uint16_t)t0;
+    int a = t0 - 1, b = t0 + 1;
+    for (int s = 1; s < n_tiles; ++s) {
+        const float da = a >= 0 ? key - thi[a] : 3.0e38f;
+        const float db = b < n_tiles ? tlo[b] - key : 3.0e38f;
+        if (da <= db) o[s] = (uint16_t)(a--);
+        else o[s] = (uint16_t)(b++);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -247,26 +538,27 @@ MADI_DEV void bitonic_clean(float (&a)[K], int (&ai)[K]) {
 }
 
 // Folds this thread's buffered (score, index) entries into ks/kj (ascending)
-// K at a time; every lane of the warp takes part.  Buffer entry e of the
-// thread lives at buf[e * EPI_THREADS].
-template <int K>
+// MB at a time; every lane of the warp takes part.  Buffer entry e of the
+// thread lives at buf[e * EPI_THREADS].  With the batch b sorted ascending and
+// padded with +inf to length K, min(ks[i], b[K-1-i]) holds the K smallest of
+// both lists as a bitonic sequence; only i >= K - MB can change.
+template <int K, int MB>
 MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, const float2* buf) {
     const int cmax = __reduce_max_sync(0xffffffffu, cnt);
 #pragma unroll 1
-    for (int base = 0; base < cmax; base += K) {
-        float b[K];
-        int bj[K];
+    for (int base = 0; base < cmax; base += MB) {
+        float b[MB];
+        int bj[MB];
 #pragma unroll
-        for (int i = 0; i < K; ++i) {
+        for (int i = 0; i < MB; ++i) {
             float2 e = make_float2(3.0e38f, 0.f);
             if (base + i < cnt) e = buf[(base + i) * EPI_THREADS];
             b[i] = e.x;
             bj[i] = __float_as_int(e.y);
         }
-        bitonic_sort<K>(b, bj);
-        // min(ks[i], b[K-1-i]) holds the K smallest of both lists, bitonic
+        bitonic_sort<MB>(b, bj);
 #pragma unroll
-        for (int i = 0; i < K; ++i) {
+        for (int i = K - MB; i < K; ++i) {
             const float o = b[K - 1 - i];
             if (o < ks[i]) { ks[i] = o; kj[i] = bj[K - 1 - i]; }
         }
@@ -276,12 +568,38 @@ MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, c
     thr = ks[K - 1];
 }
 
+// One append pass: up to four marked entries from each of two masks (column
+// offsets oa, ob within the staged keys); all eight staged loads issue before
+// the stores, so a pass costs about one load latency.
+template <int MODE>
+MADI_DEV void append_pass(uint32_t& ma, int oa, uint32_t& mb, int ob, float2*& wp, const float* stage_f, int jc) {
+    int ix[8];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        ix[u] = ma ? __ffs(ma) - 1 + oa : -1;
+        ma &= ma - 1u;
+        ix[u + 4] = mb ? __ffs(mb) - 1 + ob : -1;
+        mb &= mb - 1u;
+    }
+    float kv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) kv[u] = ix[u] >= 0 ? stage_f[(ix[u] >> 2) * (EPI_THREADS * 4) + (ix[u] & 3)] : 0.f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        if (ix[u] >= 0) {
+            *wp = make_float2(MODE == MODE_FOLD ? -2.f * kv[u] : kv[u], __int_as_float(jc + ix[u]));
+            wp += EPI_THREADS;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Main kernel: warps 0-7 are the epilogue (warpgroup h = warp / 4 takes
 // columns [64h, 64h + 64) of every tile; thread tid % 128 = voxel row = TMEM
 // lane), lane 0 of warp 8 is the producer (library loads and MMA issue).
 // Hand-offs use mbarriers only (every wait bounded):
-//   full[s]  / empty[s] : library stage s loaded / consumed by its MMA
+//   full[s]             : library stage s loaded (a stage is refilled only once
+//                         the acce wait has certified its MMA complete)
 //   accf[a]             : accumulator a holds tile scores (and, in the aux and
 //                         free modes, the tile's aux row has landed)
 //   acce[a]             : the eight epilogue warps are done with accumulator a
@@ -291,17 +609,36 @@ MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, c
 // g % STAGES, accumulator g % ACCS.  The k-th completion of a barrier is
 // waited with parity k & 1.
 // ---------------------------------------------------------------------------
+struct Plan {
+    const float* meas;
+    const float* lib;
+    int64_t n_vox;
+    int n_lib, F, n_tiles;
+    const unsigned char* tiles;         // packed library in scan order
+    const float* aux;
+    const float* mu;
+    const int32_t* vperm;               // voxel tile rows -> caller's voxel rows
+    const int32_t* lperm;               // library scan position -> caller's library rows
+    const float* lrows;                 // fp32 library rows in scan order, KPAD floats each
+    const uint16_t* order;              // [voxel tile][step] -> library tile
+    int32_t* best_idx;
+    float* best_resid;
+    float* best_s0;
+    int* err;
+};
+
 struct Smem {
     unsigned char a[A_BYTES];
     unsigned char b[STAGES][B_BYTES];
     float aux[ACCS][TILE_N];
-    float4 stage[8][EPI_THREADS];       // the 32 keys of the current chunk, 4 per slot
+    float4 stage[WG_COLS / 4][EPI_THREADS];   // the 64 keys of the current tile, 4 per slot
     float2 buf[CAP][EPI_THREADS];       // candidate buffers (score, index)
     float4 res1[2][TILE_M];             // warpgroup 1 -> 0: (resid, index, s0, -) per row
+    uint2 thr_pub[EPI_WG][TILE_M];      // (voxel tile, k-th best score) of each row and half
     uint64_t full[STAGES];
-    uint64_t empty[STAGES];
     uint64_t accf[ACCS];
     uint64_t acce[ACCS];
+    int lt_stage[STAGES];               // library tile held by each stage (producer only)
     uint64_t afull;
     uint64_t lfull;
     uint64_t drain;
@@ -314,18 +651,18 @@ MADI_DEV int err_flag_read(const Smem& S) { return *reinterpret_cast<const volat
 // Voxel tile -> BF16 canonical A rows (warpgroup 0, each thread its own row),
 // then hand the tile to the async proxy and signal the producer.
 template <int MODE>
-MADI_DEV void write_voxel_tile(Smem& S, const float* __restrict__ meas, const float* __restrict__ mu, int64_t n_vox,
-                               int F, int64_t vt, int r, int lane) {
-    const int64_t row = vt * TILE_M + r;
-    const bool live = row < n_vox;
+MADI_DEV void write_voxel_tile(Smem& S, const Plan& P, int64_t vt, int r, int lane) {
+    const int64_t pos = vt * TILE_M + r;
+    const bool live = pos < P.n_vox;
+    const int64_t row = live ? P.vperm[pos] : 0;
     for (int kc = 0; kc < KPAD / 8; ++kc) {
         __align__(16) __nv_bfloat16 v8[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int k = kc * 8 + i;
             float x = 0.f;
-            if (live && k < F) x = meas[row * F + k] - (MODE == MODE_FREE ? 0.f : __ldg(mu + k));
-            if (MODE == MODE_FOLD && k >= F && k < F + BIAS_COLS) x = 1.f;
+            if (live && k < P.F) x = P.meas[row * P.F + k] - (MODE == MODE_FREE ? 0.f : __ldg(P.mu + k));
+            if (MODE == MODE_FOLD && k >= P.F && k < P.F + BIAS_COLS) x = 1.f;
             v8[i] = __float2bfloat16_rn(x);
         }
         *reinterpret_cast<uint4*>(S.a + canon_off(r, kc * 8)) = *reinterpret_cast<const uint4*>(v8);
@@ -335,48 +672,78 @@ MADI_DEV void write_voxel_tile(Smem& S, const float* __restrict__ meas, const fl
     if (lane == 0) mbar_arrive(&S.afull);
 }
 
+// The producer is a whole warp so that the scan order can be read 32 steps at
+// a time (one coalesced load per lane, double-buffered, picked by shuffle);
+// lane 0 alone waits on barriers and issues the copies and MMAs.
 template <int MODE>
-MADI_DEV void producer(Smem& S, const unsigned char* __restrict__ tiles, const float* __restrict__ aux, int n_tiles,
-                       int64_t total, uint32_t tmem) {
+MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int lane) {
+    const int n_tiles = P.n_tiles;
+    auto order_at = [&](int64_t g) -> int {    // library tile of step g, 0 past the end
+        if (g >= total) return 0;
+        const int64_t vt = blockIdx.x + (g / n_tiles) * (int64_t)gridDim.x;
+        return (int)P.order[vt * n_tiles + (g % n_tiles)];
+    };
+    int64_t obase = 0;                           // steps [obase, obase + 32) are in ocur
+    int ocur = order_at(lane), onext = order_at(32 + lane);
+    auto lib_tile = [&](int64_t g) -> int {      // warp-uniform, g never decreases
+        while (g >= obase + 32) {
+            ocur = onext;
+            obase += 32;
+            onext = order_at(obase + 32 + lane);
+        }
+        return __shfl_sync(0xffffffffu, ocur, (int)(g - obase));
+    };
     const uint32_t idesc = make_idesc();
     const uint32_t a_base = smem_u32(S.a);
     int64_t gl = 0;                                  // library loads issued
     bool ok = true;
+    // The stage refilled with tile g + LOAD_AHEAD last held tile
+    // g + LOAD_AHEAD - STAGES <= g - ACCS; the acce wait that precedes the
+    // refill certifies the epilogue of tile g - ACCS, hence that MMA's (and all
+    // earlier MMAs') completion, so the stage is free without a barrier of its own.
+    static_assert(STAGES - LOAD_AHEAD >= ACCS, "a refilled stage must be certified free by the acce wait");
     auto load = [&](int64_t g) -> bool {
         const int st = (int)(g % STAGES);
-        if (g >= STAGES && !mbar_wait(&S.empty[st], (uint32_t)((g / STAGES - 1) & 1))) return false;
-        mbar_expect_tx(&S.full[st], B_BYTES);
-        bulk_g2s(S.b[st], tiles + (size_t)(g % n_tiles) * B_BYTES, B_BYTES, &S.full[st]);
+        const int lt = lib_tile(g);
+        if (lane == 0) {
+            S.lt_stage[st] = lt;
+            mbar_expect_tx(&S.full[st], B_BYTES);
+            bulk_g2s(S.b[st], P.tiles + (size_t)lt * B_BYTES, B_BYTES, &S.full[st]);
+        }
         return true;
     };
-    for (; gl < total && gl < STAGES; ++gl)
+    // Loads run LOAD_AHEAD tiles ahead of the MMAs: tile g + LOAD_AHEAD goes
+    // into the stage of tile g + LOAD_AHEAD - STAGES, whose MMA was issued
+    // STAGES - LOAD_AHEAD iterations earlier and has long finished, so the
+    // refill wait returns at once.
+    for (; gl < total && gl < LOAD_AHEAD; ++gl)
         if (!load(gl)) { ok = false; break; }
     for (int64_t g = 0; g < total && ok; ++g) {
         const int st = (int)(g % STAGES), acc = (int)(g % ACCS);
         const int tile = (int)(g % n_tiles);
-        if (tile == 0 && !mbar_wait(&S.afull, (uint32_t)((g / n_tiles) & 1))) { ok = false; break; }
-        if (!mbar_wait(&S.full[st], (uint32_t)((g / STAGES) & 1))) { ok = false; break; }
-        if (g >= ACCS && !mbar_wait(&S.acce[acc], (uint32_t)((g / ACCS - 1) & 1))) { ok = false; break; }
-        fence_after();
-        if (MODE != MODE_FOLD) {
-            // the tile's aux row rides on accf[acc] (arrive + tx); the MMA commit is its second arrival
-            mbar_expect_tx(&S.accf[acc], AUX_BYTES);
-            bulk_g2s(S.aux[acc], aux + (size_t)tile * TILE_N, AUX_BYTES, &S.accf[acc]);
-        }
-        const uint32_t b_base = smem_u32(S.b[st]);
-        const uint32_t d = tmem + (uint32_t)(acc * TILE_N);
-        mma_bf16(d, make_sdesc(a_base), make_sdesc(b_base), idesc, 0u);
-        mma_bf16(d, make_sdesc(a_base + 2 * LBO), make_sdesc(b_base + 2 * LBO), idesc, 1u);
-        mma_commit(&S.empty[st]);
-        mma_commit(&S.accf[acc]);
-        // refill the stage MMA g-1 used (stays STAGES-1 tiles ahead without
-        // waiting on the MMA just issued)
-        if (gl < total && gl <= g + STAGES - 1) {
+        if (g >= ACCS && !mbar_wait_warp(&S.acce[acc], (uint32_t)((g / ACCS - 1) & 1), lane)) { ok = false; break; }
+        if (gl < total && gl <= g + LOAD_AHEAD) {
             if (!load(gl)) { ok = false; break; }
             ++gl;
         }
+        if (tile == 0 && !mbar_wait_warp(&S.afull, (uint32_t)((g / n_tiles) & 1), lane)) { ok = false; break; }
+        if (!mbar_wait_warp(&S.full[st], (uint32_t)((g / STAGES) & 1), lane)) { ok = false; break; }
+        if (lane == 0) {
+            fence_after();
+            if (MODE != MODE_FOLD) {
+                // the tile's aux row rides on accf[acc] (arrive + tx); the MMA commit is its second arrival
+                mbar_expect_tx(&S.accf[acc], AUX_BYTES);
+                bulk_g2s(S.aux[acc], P.aux + (size_t)S.lt_stage[st] * TILE_N, AUX_BYTES, &S.accf[acc]);
+            }
+            const uint32_t b_base = smem_u32(S.b[st]);
+            const uint32_t d = tmem + (uint32_t)(acc * TILE_N);
+            mma_bf16(d, make_sdesc(a_base), make_sdesc(b_base), idesc, 0u);
+            mma_bf16(d, make_sdesc(a_base + 2 * LBO), make_sdesc(b_base + 2 * LBO), idesc, 1u);
+            mma_commit(&S.accf[acc]);
+        }
+        __syncwarp();
     }
-    if (!ok) {
+    if (!ok && lane == 0) {
         S.err = 1;
         // let issued copies and MMAs land before TMEM / shared memory go away
         for (int st = 0; st < STAGES; ++st) {
@@ -388,51 +755,68 @@ MADI_DEV void producer(Smem& S, const unsigned char* __restrict__ tiles, const f
     }
 }
 
-// fp32 rescore of this thread's k candidates (staged in its buffer) against
-// the fp32 data; lowest index on ties.
+// fp32 rescore of this thread's k candidates (staged in its buffer, as scan
+// positions) against the fp32 data; lowest caller index on ties.  Rows come
+// from the padded scan-order copy (at most eight aligned 16-byte loads each),
+// two candidates per step with all their loads in flight.
 template <int K, bool FREE>
-MADI_DEV void rescore(const float* __restrict__ meas, const float* __restrict__ lib, int64_t row, int n_lib, int F,
-                      const float2* mybuf, float& best, int& bj, float& bs0) {
+MADI_DEV void rescore(const Plan& P, int64_t row, const float2* mybuf, float& best, int& bj, float& bs0) {
+    const int F = P.F, nq = (F + 3) / 4;
     float m[KPAD];
 #pragma unroll
-    for (int k = 0; k < KPAD; ++k) m[k] = k < F ? meas[row * F + k] : 0.f;
-#pragma unroll 4
+    for (int k = 0; k < KPAD; ++k) m[k] = k < F ? P.meas[row * F + k] : 0.f;
+    // all K permutation lookups in flight at once; (scan position, caller index)
+    // go back into the thread's buffer slots
+    float2* wbuf = const_cast<float2*>(mybuf);
+#pragma unroll
     for (int i = 0; i < K; ++i) {
         const float2 cand = mybuf[i * EPI_THREADS];
-        const int j = __float_as_int(cand.y);
-        if (!(cand.x < 3.0e38f) || j < 0 || j >= n_lib) continue;
-        const float* L = lib + (size_t)j * F;
-        float lv[KPAD];
+        const int e = __float_as_int(cand.y);
+        const bool valid = cand.x < 3.0e38f && e >= 0 && e < P.n_lib;
+        const int j = valid ? __ldg(P.lperm + e) : -1;
+        wbuf[i * EPI_THREADS] = make_float2(__int_as_float(valid ? e : -1), __int_as_float(j));
+    }
+#pragma unroll 1
+    for (int i = 0; i < K; i += 2) {
+        int e[2], j[2];
+        float4 lv[2][KPAD / 4];
 #pragma unroll
-        for (int k = 0; k < KPAD; ++k) lv[k] = k < F ? __ldg(L + k) : 0.f;
-        float dot = 0.f, rr = 0.f;
+        for (int u = 0; u < 2; ++u) {
+            const float2 c = mybuf[(i + u) * EPI_THREADS];
+            e[u] = __float_as_int(c.x);
+            j[u] = __float_as_int(c.y);
+            const float4* L = reinterpret_cast<const float4*>(P.lrows + (size_t)(e[u] < 0 ? 0 : e[u]) * KPAD);
 #pragma unroll
-        for (int k = 0; k < KPAD; ++k)
-            if (k < F) { dot = fmaf(m[k], lv[k], dot); rr = fmaf(lv[k], lv[k], rr); }
-        const float s0 = FREE ? dot / fmaxf(rr, 1e-30f) : 1.f;
-        float res = 0.f;
+            for (int q = 0; q < KPAD / 4; ++q)
+                lv[u][q] = (e[u] >= 0 && q < nq) ? __ldg(L + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
-        for (int k = 0; k < KPAD; ++k)
-            if (k < F) { const float r = m[k] - s0 * lv[k]; res = fmaf(r, r, res); }
-        if (FREE && !(dot > 0.f)) res = 3.0e38f;
-        if (res < best || (res == best && j < bj)) { best = res; bj = j; bs0 = s0; }
+        for (int u = 0; u < 2; ++u) {
+            if (e[u] < 0) continue;
+            const float* lf = reinterpret_cast<const float*>(lv[u]);
+            float dot = 0.f, rr = 0.f;
+#pragma unroll
+            for (int k = 0; k < KPAD; ++k) { dot = fmaf(m[k], lf[k], dot); rr = fmaf(lf[k], lf[k], rr); }
+            const float s0 = FREE ? dot / fmaxf(rr, 1e-30f) : 1.f;
+            float res = 0.f;
+#pragma unroll
+            for (int k = 0; k < KPAD; ++k) { const float r = m[k] - s0 * lf[k]; res = fmaf(r, r, res); }
+            if (FREE && !(dot > 0.f)) res = 3.0e38f;
+            if (res < best || (res == best && j[u] < bj)) { best = res; bj = j[u]; bs0 = s0; }
+        }
     }
 }
 
 template <int K, int MODE>
-__global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const float* __restrict__ meas, const float* __restrict__ lib,
-                                                                int64_t n_vox, int n_lib, int F,
-                                                                const unsigned char* __restrict__ tiles,
-                                                                const float* __restrict__ aux, const float* __restrict__ mu,
-                                                                int n_tiles, int32_t* best_idx, float* best_resid,
-                                                                float* best_s0, int* err_flag) {
-    static_assert(CAP % K == 0 && CAP >= 32, "buffer holds whole merge batches and a 32-column chunk");
+__global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
+    constexpr int MB = K < 16 ? K : 16;             // merge batch
+    static_assert(CAP % MB == 0 && CAP >= 32 && CAP >= K, "buffer holds whole merge batches, a chunk and the top-k");
     constexpr bool FREE = MODE == MODE_FREE;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
-        for (int i = 0; i < STAGES; ++i) { mbar_init(&S.full[i], 1); mbar_init(&S.empty[i], 1); }
+        for (int i = 0; i < STAGES; ++i) mbar_init(&S.full[i], 1);
         for (int i = 0; i < ACCS; ++i) {
             mbar_init(&S.accf[i], MODE == MODE_FOLD ? 1 : 2);
             mbar_init(&S.acce[i], EPI_WARPS);
@@ -441,6 +825,9 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const float* __r
         mbar_init(&S.lfull, 4);
         mbar_init(&S.drain, 1);
         S.err = 0;
+    }
+    if (tid < EPI_THREADS) S.thr_pub[tid / TILE_M][tid % TILE_M] = make_uint2(0xFFFFFFFFu, 0u);
+    if (tid == 0) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -452,11 +839,12 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const float* __r
     __syncthreads();
     fence_after();
     const uint32_t tmem = S.tmem_base;
-    const int64_t n_vtiles = (n_vox + TILE_M - 1) / TILE_M;
+    const int64_t n_vtiles = (P.n_vox + TILE_M - 1) / TILE_M;
+    const int n_tiles = P.n_tiles;
     const int64_t my_vt = (int64_t)blockIdx.x < n_vtiles ? (n_vtiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
     if (warp == EPI_WARPS) {
-        if (lane == 0) producer<MODE>(S, tiles, aux, n_tiles, my_vt * n_tiles, tmem);
+        producer<MODE>(S, P, my_vt * n_tiles, tmem, lane);
     } else {
         const int wg = warp >> 2;                    // column half
         const int r = tid & (TILE_M - 1);            // voxel row = TMEM lane
@@ -466,7 +854,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const float* __r
         const float* mystage_f = reinterpret_cast<const float*>(mystage);
         int64_t g = 0;
         bool ok = true;
-        if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, meas, mu, n_vox, F, blockIdx.x, r, lane);
+        if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, P, blockIdx.x, r, lane);
         for (int64_t lv = 0; lv < my_vt && ok; ++lv) {
             const int64_t vt = blockIdx.x + lv * gridDim.x;
             float ks[K];
@@ -476,57 +864,96 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const float* __r
             float thr = 3.0e38f;
             float tthr = -1.5e38f;                   // fold mode: key t hits when t > -thr / 2
             int cnt = 0;
+            int lt_next = (int)P.order[vt * n_tiles];
             for (int t = 0; t < n_tiles; ++t, ++g) {
                 const int acc = (int)(g % ACCS);
-                const bool got_lane = mbar_wait(&S.accf[acc], (uint32_t)((g / ACCS) & 1)) && !err_flag_read(S);
-                const bool got = __all_sync(0xffffffffu, got_lane);   // warp-uniform
+                const bool got = mbar_wait_warp(&S.accf[acc], (uint32_t)((g / ACCS) & 1), lane) &&
+                                 !__any_sync(0xffffffffu, err_flag_read(S) != 0);   // warp-uniform
                 if (!got) { S.err = 1; ok = false; break; }
                 fence_after();
                 const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(acc * TILE_N + wg * WG_COLS);
                 const float* ax = S.aux[acc] + wg * WG_COLS;
-                const int jb = t * TILE_N + wg * WG_COLS;
-#pragma unroll 1
-                for (int c = 0; c < WG_COLS; c += 32) {
-                    float key[32];
-                    tmem_ld32(taddr + (uint32_t)c, key);
-                    if (MODE != MODE_FOLD) {
+                const int jb = lt_next * TILE_N + wg * WG_COLS;
+                if (t + 1 < n_tiles) lt_next = (int)P.order[vt * n_tiles + t + 1];   // prefetch the next step
+                float key[WG_COLS];
+                tmem_ld64(taddr, key);
+                if (MODE != MODE_FOLD) {
 #pragma unroll
-                        for (int i = 0; i < 32; i += 4) {
-                            const float4 q = *reinterpret_cast<const float4*>(ax + c + i);
-                            const float qq[4] = {q.x, q.y, q.z, q.w};
+                    for (int i = 0; i < WG_COLS; i += 4) {
+                        const float4 q = *reinterpret_cast<const float4*>(ax + i);
+                        const float qq[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                const float v = key[i + u];
-                                key[i + u] = FREE ? (-v * fabsf(v)) * qq[u] : fmaf(-2.f, v, qq[u]);
-                            }
+                        for (int u = 0; u < 4; ++u) {
+                            const float v = key[i + u];
+                            key[i + u] = FREE ? (-v * fabsf(v)) * qq[u] : fmaf(-2.f, v, qq[u]);
                         }
                     }
+                }
+                // An entry at or above the other half's k-th best of this row
+                // cannot be in the row's overall top-k: filter with the tighter of
+                // the two (a stale read is only looser).
+                const uint2 pp = S.thr_pub[wg ^ 1][r];
+                const float thr_e = fminf(thr, pp.x == (uint32_t)vt ? __uint_as_float(pp.y) : 3.0e38f);
+                const float tthr_e = MODE == MODE_FOLD ? fmaxf(tthr, -0.5f * thr_e) : tthr;
+                // fast path: no lane of the warp holds a candidate in this tile
+                {
+                    float ext[8];   // eight independent running extremes, then a tree
 #pragma unroll
-                    for (int i = 0; i < 32; i += 4)
+                    for (int i = 0; i < 8; ++i) ext[i] = key[i];
+#pragma unroll
+                    for (int i = 8; i < WG_COLS; ++i)
+                        ext[i & 7] = MODE == MODE_FOLD ? fmaxf(ext[i & 7], key[i]) : fminf(ext[i & 7], key[i]);
+#pragma unroll
+                    for (int w = 4; w > 0; w >>= 1)
+#pragma unroll
+                        for (int i = 0; i < w; ++i)
+                            ext[i] = MODE == MODE_FOLD ? fmaxf(ext[i], ext[i + w]) : fminf(ext[i], ext[i + w]);
+                    const bool maybe = MODE == MODE_FOLD ? ext[0] > tthr_e : ext[0] < thr_e;
+                    if (!__any_sync(0xffffffffu, maybe)) {
+                        fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&S.acce[acc]);
+                        continue;
+                    }
+                }
+                // eight independent 8-bit masks, then two 32-bit masks
+                uint32_t mk[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+                for (int i = 0; i < WG_COLS; ++i) {
+                    const bool hit = MODE == MODE_FOLD ? key[i] > tthr_e : key[i] < thr_e;
+                    if (hit) mk[i >> 3] |= 1u << (i & 7);
+                }
+                uint32_t m0 = mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24);
+                uint32_t m1 = mk[4] | (mk[5] << 8) | (mk[6] << 16) | (mk[7] << 24);
+                const int nh0 = __popc(m0), nh1 = __popc(m1);
+                if (m0 | m1) {   // stage the keys for the append passes (lanes with hits only)
+#pragma unroll
+                    for (int i = 0; i < WG_COLS; i += 4)
                         mystage[(i >> 2) * EPI_THREADS] = make_float4(key[i], key[i + 1], key[i + 2], key[i + 3]);
-                    // four independent 8-bit masks, then one 32-bit mask
-                    uint32_t mk[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) {
-                        const bool hit = MODE == MODE_FOLD ? key[i] > tthr : key[i] < thr;
-                        if (hit) mk[i >> 3] |= 1u << (i & 7);
-                    }
-                    uint32_t m = mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24);
-                    const int nh = __popc(m);
-                    if (__any_sync(0xffffffffu, cnt + nh > CAP)) {
-                        merge_buffer<K>(ks, kj, thr, cnt, mybuf);
+                }
+                float2* wp = mybuf_w + cnt * EPI_THREADS;
+                if (!__any_sync(0xffffffffu, cnt + nh0 + nh1 > CAP)) {
+                    while (__any_sync(0xffffffffu, (m0 | m1) != 0u)) append_pass<MODE>(m0, 0, m1, 32, wp, mystage_f, jb);
+                    cnt += nh0 + nh1;
+                } else {
+                    // fold before each half as needed, then append it
+                    uint32_t none = 0u;
+                    if (__any_sync(0xffffffffu, cnt + nh0 > CAP)) {
+                        merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
                         tthr = -0.5f * thr;
+                        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                        wp = mybuf_w;
                     }
-                    float2* wp = mybuf_w + cnt * EPI_THREADS;
-                    const int jc = jb + c;
-                    while (m) {
-                        const int i = __ffs(m) - 1;
-                        m &= m - 1;
-                        const float kv = mystage_f[(i >> 2) * (EPI_THREADS * 4) + (i & 3)];
-                        *wp = make_float2(MODE == MODE_FOLD ? -2.f * kv : kv, __int_as_float(jc + i));
-                        wp += EPI_THREADS;
+                    while (__any_sync(0xffffffffu, m0 != 0u)) append_pass<MODE>(m0, 0, none, 0, wp, mystage_f, jb);
+                    cnt += nh0;
+                    if (__any_sync(0xffffffffu, cnt + nh1 > CAP)) {
+                        merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
+                        tthr = -0.5f * thr;
+                        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                        wp = mybuf_w;
                     }
-                    cnt += nh;
+                    while (__any_sync(0xffffffffu, m1 != 0u)) append_pass<MODE>(m1, 32, none, 0, wp, mystage_f, jb);
+                    cnt += nh1;
                 }
                 fence_before();
                 __syncwarp();
@@ -534,30 +961,30 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const float* __r
             }
             if (!ok) break;
             // every MMA of this voxel tile is complete: the next tile's A may go in now
-            if (wg == 0 && lv + 1 < my_vt) write_voxel_tile<MODE>(S, meas, mu, n_vox, F, vt + gridDim.x, r, lane);
-            merge_buffer<K>(ks, kj, thr, cnt, mybuf);
+            if (wg == 0 && lv + 1 < my_vt) write_voxel_tile<MODE>(S, P, vt + gridDim.x, r, lane);
+            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
             // the (now empty) buffer carries the candidates to the rescore loop, so
             // ks/kj are only ever indexed by constants and stay in registers
 #pragma unroll
             for (int i = 0; i < K; ++i) mybuf_w[i * EPI_THREADS] = make_float2(ks[i], __int_as_float(kj[i]));
-            const int64_t row = vt * TILE_M + r;
+            const int64_t pos = vt * TILE_M + r;
+            const int64_t row = pos < P.n_vox ? P.vperm[pos] : -1;
             float best = 3.0e38f, bs0 = 0.f;
             int bj = 0x7FFFFFFF;
-            if (row < n_vox) rescore<K, FREE>(meas, lib, row, n_lib, F, mybuf, best, bj, bs0);
+            if (row >= 0) rescore<K, FREE>(P, row, mybuf, best, bj, bs0);
             if (wg == 1) {
                 S.res1[lv & 1][r] = make_float4(best, __int_as_float(bj), bs0, 0.f);
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.lfull);
             } else {
-                const bool got_lane = mbar_wait(&S.lfull, (uint32_t)(lv & 1));
-                if (!__all_sync(0xffffffffu, got_lane)) { S.err = 1; ok = false; break; }
+                if (!mbar_wait_warp(&S.lfull, (uint32_t)(lv & 1), lane)) { S.err = 1; ok = false; break; }
                 const float4 o = S.res1[lv & 1][r];
                 const int j1 = __float_as_int(o.y);
                 if (o.x < best || (o.x == best && j1 < bj)) { best = o.x; bj = j1; bs0 = o.z; }
-                if (row < n_vox) {
-                    best_idx[row] = bj == 0x7FFFFFFF ? 0 : bj;
-                    best_resid[row] = best;
-                    if (FREE && best_s0) best_s0[row] = bs0;
+                if (row >= 0) {
+                    P.best_idx[row] = bj == 0x7FFFFFFF ? 0 : bj;
+                    P.best_resid[row] = best;
+                    if (FREE && P.best_s0) P.best_s0[row] = bs0;
                 }
             }
         }
@@ -569,7 +996,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const float* __r
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TMEM_COLS) : "memory");
     }
-    if (tid == 0 && S.err) atomicExch(err_flag, 1);
+    if (tid == 0 && S.err) atomicExch(P.err, 1);
 }
 
 }  // namespace bf16m
@@ -580,10 +1007,51 @@ using namespace madi::bf16m;
 
 static int64_t round256(int64_t x) { return (x + 255) & ~int64_t(255); }
 
+namespace {
+// Scratch layout of the BF16 path (every part 256-byte aligned).
+struct Layout {
+    int64_t tiles, aux, mu, err, kmu, pc, cov, lkey, lperm, krange, tlo, thi;
+    int64_t lrows, vkey, vb, vrank, cnt, offs, vtot, vperm, order, total;
+};
+
+Layout layout(int64_t n_vox, int64_t n_lib) {
+    const int64_t n_tiles = (n_lib + TILE_N - 1) / TILE_N;
+    const int64_t n_vtiles = (n_vox + TILE_M - 1) / TILE_M;
+    const int64_t nblk = (n_vox + VBLK - 1) / VBLK;
+    Layout L{};
+    int64_t off = 0;
+    auto take = [&](int64_t bytes) { const int64_t o = off; off += round256(bytes); return o; };
+    L.tiles = take(n_tiles * B_BYTES);
+    L.aux = take(n_tiles * TILE_N * 4);
+    L.mu = take(KPAD * 4);
+    L.err = take(4);
+    L.kmu = take(KPAD * 4);
+    L.pc = take(KPAD * 4);
+    L.cov = take(KPAD * KPAD * 4);
+    L.lkey = take(n_lib * 4);
+    L.lperm = take(n_lib * 4);
+    L.krange = take(8);
+    L.tlo = take(n_tiles * 4);
+    L.thi = take(n_tiles * 4);
+    L.lrows = take(n_lib * KPAD * 4);
+    L.vkey = take(n_vox * 4);
+    L.vb = take(n_vox);
+    L.vrank = take(n_vox * 2);
+    L.cnt = take(nblk * NBUCKET * 4);
+    L.offs = take(nblk * NBUCKET * 4);
+    L.vtot = take(NBUCKET * 4);
+    L.vperm = take(n_vox * 4);
+    L.order = take(n_vtiles * n_tiles * 2);
+    L.total = off;
+    return L;
+}
+
+unsigned blocks_for(int64_t n, int per) { return (unsigned)((n + per - 1) / per); }
+}  // namespace
+
 int64_t madi_match_bf16_scratch(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t topk) {
-    (void)n_vox; (void)n_feat; (void)topk;
-    const int64_t n_tiles = ((int64_t)n_lib + TILE_N - 1) / TILE_N;
-    return round256(n_tiles * B_BYTES) + round256(n_tiles * TILE_N * 4) + round256(KPAD * 4) + 256;
+    (void)n_feat; (void)topk;
+    return layout(n_vox, n_lib).total;
 }
 
 // Library column means (fp64 sums), shared with the fp32 fixed-S0 scan.
@@ -594,30 +1062,96 @@ void madi_match_column_mean(const float* lib, int32_t n_lib, int32_t n_feat, flo
 madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     if (d->topk != 8 && d->topk != 16 && d->topk != 32)
         return host::fail(MADI_ERR_UNSUPPORTED, "match bf16: topk must be 8, 16 or 32");
-    const int64_t need = madi_match_bf16_scratch(d->n_vox, d->n_lib, d->n_feat, d->topk);
-    if (!d->scratch || d->scratch_bytes < need)
+    const int64_t n_tiles64 = ((int64_t)d->n_lib + TILE_N - 1) / TILE_N;
+    if (d->n_vox >= (int64_t(1) << 31) || n_tiles64 > 65535)
+        return host::fail(MADI_ERR_UNSUPPORTED, "match bf16: at most 2^31-1 voxels and 65535 library tiles");
+    const Layout Ly = layout(d->n_vox, d->n_lib);
+    if (!d->scratch || d->scratch_bytes < Ly.total)
         return host::fail(MADI_ERR_CAPACITY, "match bf16: scratch %lld < %lld bytes", (long long)d->scratch_bytes,
-                          (long long)need);
+                          (long long)Ly.total);
     if ((reinterpret_cast<uintptr_t>(d->scratch) & 255) != 0)
         return host::fail(MADI_ERR_INVALID, "match bf16: scratch must be 256-byte aligned");
-    const int n_tiles = (d->n_lib + TILE_N - 1) / TILE_N;
     unsigned char* base = static_cast<unsigned char*>(d->scratch);
-    unsigned char* tiles = base;
-    float* aux = reinterpret_cast<float*>(base + round256((int64_t)n_tiles * B_BYTES));
-    float* mu = reinterpret_cast<float*>(base + round256((int64_t)n_tiles * B_BYTES) + round256((int64_t)n_tiles * TILE_N * 4));
-    int* err = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(mu) + round256(KPAD * 4));
+    auto at = [&](int64_t off) { return base + off; };
+    const int n_tiles = (int)n_tiles64;
+    const int64_t n_vox = d->n_vox, n_vtiles = (n_vox + TILE_M - 1) / TILE_M, nblk = (n_vox + VBLK - 1) / VBLK;
+    const int n_lib = d->n_lib, F = d->n_feat;
     const bool free_s0 = d->mode == MADI_MATCH_FREE_S0;
-    const int mode = free_s0 ? MODE_FREE : (d->n_feat + BIAS_COLS <= KPAD ? MODE_FOLD : MODE_AUX);
+    const int mode = free_s0 ? MODE_FREE : (F + BIAS_COLS <= KPAD ? MODE_FOLD : MODE_AUX);
+    const int unit = free_s0 ? 1 : 0;
+    float* mu = reinterpret_cast<float*>(at(Ly.mu));
+    float* kmu = reinterpret_cast<float*>(at(Ly.kmu));
+    float* pc = reinterpret_cast<float*>(at(Ly.pc));
+    float* cov = reinterpret_cast<float*>(at(Ly.cov));
+    float* lkey = reinterpret_cast<float*>(at(Ly.lkey));
+    int32_t* lperm = reinterpret_cast<int32_t*>(at(Ly.lperm));
+    float* krange = reinterpret_cast<float*>(at(Ly.krange));
+    float* tlo = reinterpret_cast<float*>(at(Ly.tlo));
+    float* thi = reinterpret_cast<float*>(at(Ly.thi));
+    float* vkey = reinterpret_cast<float*>(at(Ly.vkey));
+    uint8_t* vb = reinterpret_cast<uint8_t*>(at(Ly.vb));
+    uint16_t* vrank = reinterpret_cast<uint16_t*>(at(Ly.vrank));
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(at(Ly.cnt));
+    uint32_t* offs = reinterpret_cast<uint32_t*>(at(Ly.offs));
+    int32_t* vperm = reinterpret_cast<int32_t*>(at(Ly.vperm));
+    uint16_t* order = reinterpret_cast<uint16_t*>(at(Ly.order));
+    int* err = reinterpret_cast<int*>(at(Ly.err));
+
     cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), s);
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");
-    if (!free_s0) column_mean_kernel<<<d->n_feat, 256, 0, s>>>(d->lib, d->n_lib, d->n_feat, mu);
-    const int64_t n_ent = (int64_t)n_tiles * TILE_N;
-    pack_library_kernel<<<(unsigned)((n_ent + 255) / 256), 256, 0, s>>>(d->lib, d->n_lib, d->n_feat, n_tiles, mode, mu,
-                                                                         tiles, aux);
+    if (!free_s0) column_mean_kernel<<<F, 256, 0, s>>>(d->lib, n_lib, F, mu);
+    // ---- scan order: library sorted along its principal axis, voxels bucketed ----
+    const bool sorted = n_lib <= SORT_MAX;
+    if (sorted) {
+        key_mean_kernel<<<F, 256, 0, s>>>(d->lib, n_lib, F, unit, kmu);
+        key_cov_kernel<<<F * F, 256, 0, s>>>(d->lib, n_lib, F, unit, kmu, cov);
+        key_axis_kernel<<<1, 32, 0, s>>>(cov, F, pc);
+        key_kernel<<<blocks_for(n_lib, 256), 256, 0, s>>>(d->lib, n_lib, F, unit, kmu, pc, lkey);
+        int n2 = 1;
+        while (n2 < n_lib) n2 <<= 1;
+        e = cudaFuncSetAttribute(lib_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SORT_MAX * 4);
+        if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 sort attribute");
+        lib_sort_kernel<<<1, 1024, (size_t)n2 * 4, s>>>(lkey, n_lib, lperm, krange);
+        tile_bounds_kernel<<<blocks_for(n_tiles, 256), 256, 0, s>>>(lkey, lperm, n_lib, n_tiles, tlo, thi);
+        vox_bucket_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(d->measured, n_vox, F, unit, kmu, pc, krange, vkey, vb);
+        vox_rank_kernel<<<(unsigned)nblk, VBLK, 0, s>>>(vb, n_vox, vrank, cnt);
+        uint32_t* vtot = reinterpret_cast<uint32_t*>(at(Ly.vtot));
+        vox_scan_kernel<<<NBUCKET, 1024, 0, s>>>(cnt, (int)nblk, offs, vtot);
+        vox_base_kernel<<<1, 32, 0, s>>>(vtot);
+        vox_scatter_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(vb, vrank, offs, vtot, n_vox, (int)nblk, vperm);
+    } else {
+        iota_kernel<<<blocks_for(n_lib, 256), 256, 0, s>>>(lperm, n_lib);
+        iota_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(vperm, n_vox);
+    }
+    order_kernel<<<blocks_for(n_vtiles, 128), 128, 0, s>>>(vkey, vperm, n_vox, n_vtiles, tlo, thi, n_tiles,
+                                                            sorted ? 1 : 0, order);
+    pack_library_kernel<<<blocks_for((int64_t)n_tiles * TILE_N, 256), 256, 0, s>>>(
+        d->lib, n_lib, F, n_tiles, mode, mu, lperm, reinterpret_cast<unsigned char*>(at(Ly.tiles)),
+        reinterpret_cast<float*>(at(Ly.aux)), reinterpret_cast<float*>(at(Ly.lrows)));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 preparation");
+
+    Plan P{};
+    P.meas = d->measured;
+    P.lib = d->lib;
+    P.n_vox = n_vox;
+    P.n_lib = n_lib;
+    P.F = F;
+    P.n_tiles = n_tiles;
+    P.tiles = reinterpret_cast<const unsigned char*>(at(Ly.tiles));
+    P.aux = reinterpret_cast<const float*>(at(Ly.aux));
+    P.mu = mu;
+    P.vperm = vperm;
+    P.lperm = lperm;
+    P.lrows = reinterpret_cast<const float*>(at(Ly.lrows));
+    P.order = order;
+    P.best_idx = d->best_idx;
+    P.best_resid = d->best_resid;
+    P.best_s0 = d->best_s0;
+    P.err = err;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t n_vtiles = (d->n_vox + TILE_M - 1) / TILE_M;
     const size_t smem = sizeof(Smem);
     // one CTA per SM: it allocates all 512 TMEM columns
     const int grid = (int)std::min<int64_t>(n_vtiles, (int64_t)sms);
@@ -626,8 +1160,7 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
         auto k = match_bf16_kernel<KK, MD>;                                                               \
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);             \
         if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 attribute");                          \
-        k<<<grid, THREADS, smem, s>>>(d->measured, d->lib, d->n_vox, d->n_lib, d->n_feat, tiles, aux, mu, \
-                                      n_tiles, d->best_idx, d->best_resid, d->best_s0, err);              \
+        k<<<grid, THREADS, smem, s>>>(P);                                                                 \
     } while (0)
 #define MADI_LAUNCH_BF16_K(MD)                                                                            \
     do {                                                                                                  \
