@@ -45,15 +45,17 @@ constexpr int LBO = CORE;                       // 128 B between K-adjacent core
 constexpr int A_BYTES = TILE_M * KPAD * 2;      // 8 KB
 constexpr int B_BYTES = TILE_N * KPAD * 2;      // 8 KB
 constexpr int AUX_BYTES = TILE_N * 4;           // per-entry |L~|^2 (aux mode) or 1/|r~|^2 (free)
-constexpr int STAGES = 8;                       // library tiles in flight
-constexpr int LOAD_AHEAD = 4;                   // library tiles loaded ahead of the MMA
-constexpr int ACCS = 4;                         // TMEM accumulators
-constexpr int TMEM_COLS = ACCS * TILE_N;        // 512: the whole TMEM of the SM
+constexpr int PAIR = 2;                         // library tiles per step (one N=256 MMA)
+constexpr int MMA_N = PAIR * TILE_N;            // 256
+constexpr int STAGES = 4;                       // steps (tile pairs) in flight
+constexpr int LOAD_AHEAD = 2;                   // steps loaded ahead of the MMA
+constexpr int ACCS = 2;                         // TMEM accumulators of MMA_N columns
+constexpr int TMEM_COLS = ACCS * MMA_N;         // 512: the whole TMEM of the SM
 constexpr int EPI_WG = 2;                       // epilogue warpgroups (column halves)
 constexpr int EPI_THREADS = EPI_WG * TILE_M;    // 256
 constexpr int EPI_WARPS = EPI_THREADS / 32;     // 8
 constexpr int THREADS = EPI_THREADS + 32;       // + producer warp
-constexpr int WG_COLS = TILE_N / EPI_WG;        // 64 columns per warpgroup and tile
+constexpr int WG_COLS = 64;                     // columns per epilogue pass (two per step)
 constexpr int CAP = 32;                         // per-thread candidate buffer entries
 constexpr uint32_t SUSPEND_NS = 20000;          // mbarrier try_wait suspend hint
 constexpr uint32_t SPIN_LIMIT = 50000;          // bounded waits: <= SPIN_LIMIT * SUSPEND_NS ~ 1 s
@@ -77,13 +79,13 @@ MADI_DEV uint64_t make_sdesc(uint32_t saddr) {
     return d;                                   // base offset 0, layout type 0 = no swizzle
 }
 
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N = 128, M = 128.
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N = 256, M = 128.
 MADI_DEV uint32_t make_idesc() {
     uint32_t d = 0;
     d |= 1u << 4;                               // D format F32
     d |= 1u << 7;                               // A format BF16
     d |= 1u << 10;                              // B format BF16
-    d |= (uint32_t)(TILE_N >> 3) << 17;         // N >> 3
+    d |= (uint32_t)(MMA_N >> 3) << 17;          // N >> 3
     d |= (uint32_t)(TILE_M >> 4) << 24;         // M >> 4
     return d;
 }
@@ -629,8 +631,8 @@ struct Plan {
 
 struct Smem {
     unsigned char a[A_BYTES];
-    unsigned char b[STAGES][B_BYTES];
-    float aux[ACCS][TILE_N];
+    unsigned char b[STAGES][PAIR * B_BYTES];     // a step's two tiles back to back = one 256-row operand
+    float aux[ACCS][PAIR][TILE_N];
     float4 stage[WG_COLS / 4][EPI_THREADS];   // the 64 keys of the current tile, 4 per slot
     float2 buf[CAP][EPI_THREADS];       // candidate buffers (score, index)
     float4 res1[2][TILE_M];             // warpgroup 1 -> 0: (resid, index, s0, -) per row
@@ -638,7 +640,7 @@ struct Smem {
     uint64_t full[STAGES];
     uint64_t accf[ACCS];
     uint64_t acce[ACCS];
-    int lt_stage[STAGES];               // library tile held by each stage (producer only)
+    int lt_stage[STAGES][PAIR];         // library tiles held by each stage (producer only)
     uint64_t afull;
     uint64_t lfull;
     uint64_t drain;
@@ -672,71 +674,69 @@ MADI_DEV void write_voxel_tile(Smem& S, const Plan& P, int64_t vt, int r, int la
     if (lane == 0) mbar_arrive(&S.afull);
 }
 
-// The producer is a whole warp so that the scan order can be read 32 steps at
+// The producer is a whole warp so that the scan order can be read 32 tiles at
 // a time (one coalesced load per lane, double-buffered, picked by shuffle);
-// lane 0 alone waits on barriers and issues the copies and MMAs.
+// lane 0 alone waits on barriers and issues the copies and MMAs.  Step g
+// covers tiles 2g and 2g + 1 of the padded per-voxel-tile sequence (an odd
+// tile count is padded with the all-padding tile n_tiles).
 template <int MODE>
 MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int lane) {
-    const int n_tiles = P.n_tiles;
-    auto order_at = [&](int64_t g) -> int {    // library tile of step g, 0 past the end
-        if (g >= total) return 0;
-        const int64_t vt = blockIdx.x + (g / n_tiles) * (int64_t)gridDim.x;
-        return (int)P.order[vt * n_tiles + (g % n_tiles)];
+    const int n_tiles = P.n_tiles, n_pad = PAIR * ((n_tiles + PAIR - 1) / PAIR);
+    const int64_t n_q = total * PAIR;
+    auto order_at = [&](int64_t q) -> int {    // library tile of padded position q, 0 past the end
+        if (q >= n_q) return 0;
+        const int64_t vt = blockIdx.x + (q / n_pad) * (int64_t)gridDim.x;
+        const int i = (int)(q % n_pad);
+        return i < n_tiles ? (int)P.order[vt * n_tiles + i] : n_tiles;
     };
-    int64_t obase = 0;                           // steps [obase, obase + 32) are in ocur
+    int64_t obase = 0;                           // positions [obase, obase + 32) are in ocur
     int ocur = order_at(lane), onext = order_at(32 + lane);
-    auto lib_tile = [&](int64_t g) -> int {      // warp-uniform, g never decreases
-        while (g >= obase + 32) {
+    auto lib_tile = [&](int64_t q) -> int {      // warp-uniform, q never decreases
+        while (q >= obase + 32) {
             ocur = onext;
             obase += 32;
             onext = order_at(obase + 32 + lane);
         }
-        return __shfl_sync(0xffffffffu, ocur, (int)(g - obase));
+        return __shfl_sync(0xffffffffu, ocur, (int)(q - obase));
     };
     const uint32_t idesc = make_idesc();
     const uint32_t a_base = smem_u32(S.a);
-    int64_t gl = 0;                                  // library loads issued
+    int64_t gl = 0;                                  // steps loaded
     bool ok = true;
-    // The stage refilled with tile g + LOAD_AHEAD last held tile
+    // The stage refilled with step g + LOAD_AHEAD last held step
     // g + LOAD_AHEAD - STAGES <= g - ACCS; the acce wait that precedes the
-    // refill certifies the epilogue of tile g - ACCS, hence that MMA's (and all
+    // refill certifies the epilogue of step g - ACCS, hence that MMA's (and all
     // earlier MMAs') completion, so the stage is free without a barrier of its own.
     static_assert(STAGES - LOAD_AHEAD >= ACCS, "a refilled stage must be certified free by the acce wait");
-    auto load = [&](int64_t g) -> bool {
+    auto load = [&](int64_t g) {
         const int st = (int)(g % STAGES);
-        const int lt = lib_tile(g);
+        const int lt0 = lib_tile(PAIR * g), lt1 = lib_tile(PAIR * g + 1);
         if (lane == 0) {
-            S.lt_stage[st] = lt;
-            mbar_expect_tx(&S.full[st], B_BYTES);
-            bulk_g2s(S.b[st], P.tiles + (size_t)lt * B_BYTES, B_BYTES, &S.full[st]);
+            S.lt_stage[st][0] = lt0;
+            S.lt_stage[st][1] = lt1;
+            mbar_expect_tx(&S.full[st], PAIR * B_BYTES);
+            bulk_g2s(S.b[st], P.tiles + (size_t)lt0 * B_BYTES, B_BYTES, &S.full[st]);
+            bulk_g2s(S.b[st] + B_BYTES, P.tiles + (size_t)lt1 * B_BYTES, B_BYTES, &S.full[st]);
         }
-        return true;
     };
-    // Loads run LOAD_AHEAD tiles ahead of the MMAs: tile g + LOAD_AHEAD goes
-    // into the stage of tile g + LOAD_AHEAD - STAGES, whose MMA was issued
-    // STAGES - LOAD_AHEAD iterations earlier and has long finished, so the
-    // refill wait returns at once.
-    for (; gl < total && gl < LOAD_AHEAD; ++gl)
-        if (!load(gl)) { ok = false; break; }
+    const int64_t n_steps = n_pad / PAIR;
+    for (; gl < total && gl < LOAD_AHEAD; ++gl) load(gl);
     for (int64_t g = 0; g < total && ok; ++g) {
         const int st = (int)(g % STAGES), acc = (int)(g % ACCS);
-        const int tile = (int)(g % n_tiles);
         if (g >= ACCS && !mbar_wait_warp(&S.acce[acc], (uint32_t)((g / ACCS - 1) & 1), lane)) { ok = false; break; }
-        if (gl < total && gl <= g + LOAD_AHEAD) {
-            if (!load(gl)) { ok = false; break; }
-            ++gl;
-        }
-        if (tile == 0 && !mbar_wait_warp(&S.afull, (uint32_t)((g / n_tiles) & 1), lane)) { ok = false; break; }
+        if (gl < total && gl <= g + LOAD_AHEAD) load(gl++);
+        if (g % n_steps == 0 && !mbar_wait_warp(&S.afull, (uint32_t)((g / n_steps) & 1), lane)) { ok = false; break; }
         if (!mbar_wait_warp(&S.full[st], (uint32_t)((g / STAGES) & 1), lane)) { ok = false; break; }
         if (lane == 0) {
             fence_after();
             if (MODE != MODE_FOLD) {
-                // the tile's aux row rides on accf[acc] (arrive + tx); the MMA commit is its second arrival
-                mbar_expect_tx(&S.accf[acc], AUX_BYTES);
-                bulk_g2s(S.aux[acc], P.aux + (size_t)S.lt_stage[st] * TILE_N, AUX_BYTES, &S.accf[acc]);
+                // the step's aux rows ride on accf[acc] (arrive + tx); the MMA commit is its second arrival
+                mbar_expect_tx(&S.accf[acc], PAIR * AUX_BYTES);
+                bulk_g2s(S.aux[acc][0], P.aux + (size_t)S.lt_stage[st][0] * TILE_N, AUX_BYTES, &S.accf[acc]);
+                bulk_g2s(S.aux[acc][1], P.aux + (size_t)S.lt_stage[st][1] * TILE_N, AUX_BYTES, &S.accf[acc]);
             }
             const uint32_t b_base = smem_u32(S.b[st]);
-            const uint32_t d = tmem + (uint32_t)(acc * TILE_N);
+            const uint32_t d = tmem + (uint32_t)(acc * MMA_N);
             mma_bf16(d, make_sdesc(a_base), make_sdesc(b_base), idesc, 0u);
             mma_bf16(d, make_sdesc(a_base + 2 * LBO), make_sdesc(b_base + 2 * LBO), idesc, 1u);
             mma_commit(&S.accf[acc]);
@@ -841,10 +841,11 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
     const uint32_t tmem = S.tmem_base;
     const int64_t n_vtiles = (P.n_vox + TILE_M - 1) / TILE_M;
     const int n_tiles = P.n_tiles;
+    const int n_steps = (n_tiles + PAIR - 1) / PAIR;
     const int64_t my_vt = (int64_t)blockIdx.x < n_vtiles ? (n_vtiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
     if (warp == EPI_WARPS) {
-        producer<MODE>(S, P, my_vt * n_tiles, tmem, lane);
+        producer<MODE>(S, P, my_vt * n_steps, tmem, lane);
     } else {
         const int wg = warp >> 2;                    // column half
         const int r = tid & (TILE_M - 1);            // voxel row = TMEM lane
@@ -864,96 +865,101 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
             float thr = 3.0e38f;
             float tthr = -1.5e38f;                   // fold mode: key t hits when t > -thr / 2
             int cnt = 0;
-            int lt_next = (int)P.order[vt * n_tiles];
-            for (int t = 0; t < n_tiles; ++t, ++g) {
+            // library tile of this warpgroup at step t (the padding tile past the end)
+            auto my_tile = [&](int t) -> int {
+                const int i = PAIR * t + wg;
+                return i < n_tiles ? (int)P.order[vt * n_tiles + i] : n_tiles;
+            };
+            int lt_next = my_tile(0);
+            for (int t = 0; t < n_steps; ++t, ++g) {
                 const int acc = (int)(g % ACCS);
                 const bool got = mbar_wait_warp(&S.accf[acc], (uint32_t)((g / ACCS) & 1), lane) &&
                                  !__any_sync(0xffffffffu, err_flag_read(S) != 0);   // warp-uniform
                 if (!got) { S.err = 1; ok = false; break; }
                 fence_after();
-                const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(acc * TILE_N + wg * WG_COLS);
-                const float* ax = S.aux[acc] + wg * WG_COLS;
-                const int jb = lt_next * TILE_N + wg * WG_COLS;
-                if (t + 1 < n_tiles) lt_next = (int)P.order[vt * n_tiles + t + 1];   // prefetch the next step
-                float key[WG_COLS];
-                tmem_ld64(taddr, key);
-                if (MODE != MODE_FOLD) {
-#pragma unroll
-                    for (int i = 0; i < WG_COLS; i += 4) {
-                        const float4 q = *reinterpret_cast<const float4*>(ax + i);
-                        const float qq[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const float v = key[i + u];
-                            key[i + u] = FREE ? (-v * fabsf(v)) * qq[u] : fmaf(-2.f, v, qq[u]);
+                const int lt = lt_next;
+                if (t + 1 < n_steps) lt_next = my_tile(t + 1);   // prefetch the next step
+                const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(acc * MMA_N + wg * TILE_N);
+#pragma unroll 1
+                for (int c = 0; c < TILE_N; c += WG_COLS) {
+                const uint32_t taddr = tbase + (uint32_t)c;
+                const float* ax = S.aux[acc][wg] + c;
+                const int jb = lt * TILE_N + c;
+                    float key[WG_COLS];
+                    tmem_ld64(taddr, key);
+                    if (MODE != MODE_FOLD) {
+    #pragma unroll
+                        for (int i = 0; i < WG_COLS; i += 4) {
+                            const float4 q = *reinterpret_cast<const float4*>(ax + i);
+                            const float qq[4] = {q.x, q.y, q.z, q.w};
+    #pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                const float v = key[i + u];
+                                key[i + u] = FREE ? (-v * fabsf(v)) * qq[u] : fmaf(-2.f, v, qq[u]);
+                            }
                         }
                     }
-                }
-                // An entry at or above the other half's k-th best of this row
-                // cannot be in the row's overall top-k: filter with the tighter of
-                // the two (a stale read is only looser).
-                const uint2 pp = S.thr_pub[wg ^ 1][r];
-                const float thr_e = fminf(thr, pp.x == (uint32_t)vt ? __uint_as_float(pp.y) : 3.0e38f);
-                const float tthr_e = MODE == MODE_FOLD ? fmaxf(tthr, -0.5f * thr_e) : tthr;
-                // fast path: no lane of the warp holds a candidate in this tile
-                {
-                    float ext[8];   // eight independent running extremes, then a tree
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) ext[i] = key[i];
-#pragma unroll
-                    for (int i = 8; i < WG_COLS; ++i)
-                        ext[i & 7] = MODE == MODE_FOLD ? fmaxf(ext[i & 7], key[i]) : fminf(ext[i & 7], key[i]);
-#pragma unroll
-                    for (int w = 4; w > 0; w >>= 1)
-#pragma unroll
-                        for (int i = 0; i < w; ++i)
-                            ext[i] = MODE == MODE_FOLD ? fmaxf(ext[i], ext[i + w]) : fminf(ext[i], ext[i + w]);
-                    const bool maybe = MODE == MODE_FOLD ? ext[0] > tthr_e : ext[0] < thr_e;
-                    if (!__any_sync(0xffffffffu, maybe)) {
-                        fence_before();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(&S.acce[acc]);
-                        continue;
+                    // An entry at or above the other half's k-th best of this row
+                    // cannot be in the row's overall top-k: filter with the tighter of
+                    // the two (a stale read is only looser).
+                    const uint2 pp = S.thr_pub[wg ^ 1][r];
+                    const float thr_e = fminf(thr, pp.x == (uint32_t)vt ? __uint_as_float(pp.y) : 3.0e38f);
+                    const float tthr_e = MODE == MODE_FOLD ? fmaxf(tthr, -0.5f * thr_e) : tthr;
+                    // fast path: no lane of the warp holds a candidate in this tile
+                    {
+                        float ext[8];   // eight independent running extremes, then a tree
+    #pragma unroll
+                        for (int i = 0; i < 8; ++i) ext[i] = key[i];
+    #pragma unroll
+                        for (int i = 8; i < WG_COLS; ++i)
+                            ext[i & 7] = MODE == MODE_FOLD ? fmaxf(ext[i & 7], key[i]) : fminf(ext[i & 7], key[i]);
+    #pragma unroll
+                        for (int w = 4; w > 0; w >>= 1)
+    #pragma unroll
+                            for (int i = 0; i < w; ++i)
+                                ext[i] = MODE == MODE_FOLD ? fmaxf(ext[i], ext[i + w]) : fminf(ext[i], ext[i + w]);
+                        const bool maybe = MODE == MODE_FOLD ? ext[0] > tthr_e : ext[0] < thr_e;
+                        if (!__any_sync(0xffffffffu, maybe)) continue;   // nothing for this warp here
                     }
-                }
-                // eight independent 8-bit masks, then two 32-bit masks
-                uint32_t mk[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-#pragma unroll
-                for (int i = 0; i < WG_COLS; ++i) {
-                    const bool hit = MODE == MODE_FOLD ? key[i] > tthr_e : key[i] < thr_e;
-                    if (hit) mk[i >> 3] |= 1u << (i & 7);
-                }
-                uint32_t m0 = mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24);
-                uint32_t m1 = mk[4] | (mk[5] << 8) | (mk[6] << 16) | (mk[7] << 24);
-                const int nh0 = __popc(m0), nh1 = __popc(m1);
-                if (m0 | m1) {   // stage the keys for the append passes (lanes with hits only)
-#pragma unroll
-                    for (int i = 0; i < WG_COLS; i += 4)
-                        mystage[(i >> 2) * EPI_THREADS] = make_float4(key[i], key[i + 1], key[i + 2], key[i + 3]);
-                }
-                float2* wp = mybuf_w + cnt * EPI_THREADS;
-                if (!__any_sync(0xffffffffu, cnt + nh0 + nh1 > CAP)) {
-                    while (__any_sync(0xffffffffu, (m0 | m1) != 0u)) append_pass<MODE>(m0, 0, m1, 32, wp, mystage_f, jb);
-                    cnt += nh0 + nh1;
-                } else {
-                    // fold before each half as needed, then append it
-                    uint32_t none = 0u;
-                    if (__any_sync(0xffffffffu, cnt + nh0 > CAP)) {
-                        merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
-                        tthr = -0.5f * thr;
-                        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
-                        wp = mybuf_w;
+                    // eight independent 8-bit masks, then two 32-bit masks
+                    uint32_t mk[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+    #pragma unroll
+                    for (int i = 0; i < WG_COLS; ++i) {
+                        const bool hit = MODE == MODE_FOLD ? key[i] > tthr_e : key[i] < thr_e;
+                        if (hit) mk[i >> 3] |= 1u << (i & 7);
                     }
-                    while (__any_sync(0xffffffffu, m0 != 0u)) append_pass<MODE>(m0, 0, none, 0, wp, mystage_f, jb);
-                    cnt += nh0;
-                    if (__any_sync(0xffffffffu, cnt + nh1 > CAP)) {
-                        merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
-                        tthr = -0.5f * thr;
-                        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
-                        wp = mybuf_w;
+                    uint32_t m0 = mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24);
+                    uint32_t m1 = mk[4] | (mk[5] << 8) | (mk[6] << 16) | (mk[7] << 24);
+                    const int nh0 = __popc(m0), nh1 = __popc(m1);
+                    if (m0 | m1) {   // stage the keys for the append passes (lanes with hits only)
+    #pragma unroll
+                        for (int i = 0; i < WG_COLS; i += 4)
+                            mystage[(i >> 2) * EPI_THREADS] = make_float4(key[i], key[i + 1], key[i + 2], key[i + 3]);
                     }
-                    while (__any_sync(0xffffffffu, m1 != 0u)) append_pass<MODE>(m1, 32, none, 0, wp, mystage_f, jb);
-                    cnt += nh1;
+                    float2* wp = mybuf_w + cnt * EPI_THREADS;
+                    if (!__any_sync(0xffffffffu, cnt + nh0 + nh1 > CAP)) {
+                        while (__any_sync(0xffffffffu, (m0 | m1) != 0u)) append_pass<MODE>(m0, 0, m1, 32, wp, mystage_f, jb);
+                        cnt += nh0 + nh1;
+                    } else {
+                        // fold before each half as needed, then append it
+                        uint32_t none = 0u;
+                        if (__any_sync(0xffffffffu, cnt + nh0 > CAP)) {
+                            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
+                            tthr = -0.5f * thr;
+                            S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                            wp = mybuf_w;
+                        }
+                        while (__any_sync(0xffffffffu, m0 != 0u)) append_pass<MODE>(m0, 0, none, 0, wp, mystage_f, jb);
+                        cnt += nh0;
+                        if (__any_sync(0xffffffffu, cnt + nh1 > CAP)) {
+                            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
+                            tthr = -0.5f * thr;
+                            S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                            wp = mybuf_w;
+                        }
+                        while (__any_sync(0xffffffffu, m1 != 0u)) append_pass<MODE>(m1, 32, none, 0, wp, mystage_f, jb);
+                        cnt += nh1;
+                    }
                 }
                 fence_before();
                 __syncwarp();
@@ -1016,13 +1022,14 @@ struct Layout {
 
 Layout layout(int64_t n_vox, int64_t n_lib) {
     const int64_t n_tiles = (n_lib + TILE_N - 1) / TILE_N;
+    const int64_t n_pad = PAIR * ((n_tiles + PAIR - 1) / PAIR);   // + the all-padding tile when odd
     const int64_t n_vtiles = (n_vox + TILE_M - 1) / TILE_M;
     const int64_t nblk = (n_vox + VBLK - 1) / VBLK;
     Layout L{};
     int64_t off = 0;
     auto take = [&](int64_t bytes) { const int64_t o = off; off += round256(bytes); return o; };
-    L.tiles = take(n_tiles * B_BYTES);
-    L.aux = take(n_tiles * TILE_N * 4);
+    L.tiles = take(n_pad * B_BYTES);
+    L.aux = take(n_pad * TILE_N * 4);
     L.mu = take(KPAD * 4);
     L.err = take(4);
     L.kmu = take(KPAD * 4);
@@ -1125,8 +1132,9 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     }
     order_kernel<<<blocks_for(n_vtiles, 128), 128, 0, s>>>(vkey, vperm, n_vox, n_vtiles, tlo, thi, n_tiles,
                                                             sorted ? 1 : 0, order);
-    pack_library_kernel<<<blocks_for((int64_t)n_tiles * TILE_N, 256), 256, 0, s>>>(
-        d->lib, n_lib, F, n_tiles, mode, mu, lperm, reinterpret_cast<unsigned char*>(at(Ly.tiles)),
+    const int n_pad = PAIR * ((n_tiles + PAIR - 1) / PAIR);
+    pack_library_kernel<<<blocks_for((int64_t)n_pad * TILE_N, 256), 256, 0, s>>>(
+        d->lib, n_lib, F, n_pad, mode, mu, lperm, reinterpret_cast<unsigned char*>(at(Ly.tiles)),
         reinterpret_cast<float*>(at(Ly.aux)), reinterpret_cast<float*>(at(Ly.lrows)));
     e = cudaGetLastError();
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 preparation");
