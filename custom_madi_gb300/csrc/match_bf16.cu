@@ -760,7 +760,7 @@ MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int
 // from the padded scan-order copy (at most eight aligned 16-byte loads each),
 // two candidates per step with all their loads in flight.
 template <int K, bool FREE>
-MADI_DEV void rescore(const Plan& P, int64_t row, const float2* mybuf, float& best, int& bj, float& bs0) {
+MADI_DEV void rescore(const Plan& P, int64_t row, const float2* mybuf, int nv, float& best, int& bj, float& bs0) {
     const int F = P.F, nq = (F + 3) / 4;
     float m[KPAD];
 #pragma unroll
@@ -772,12 +772,12 @@ MADI_DEV void rescore(const Plan& P, int64_t row, const float2* mybuf, float& be
     for (int i = 0; i < K; ++i) {
         const float2 cand = mybuf[i * EPI_THREADS];
         const int e = __float_as_int(cand.y);
-        const bool valid = cand.x < 3.0e38f && e >= 0 && e < P.n_lib;
+        const bool valid = i < nv && cand.x < 3.0e38f && e >= 0 && e < P.n_lib;
         const int j = valid ? __ldg(P.lperm + e) : -1;
         wbuf[i * EPI_THREADS] = make_float2(__int_as_float(valid ? e : -1), __int_as_float(j));
     }
 #pragma unroll 1
-    for (int i = 0; i < K; i += 2) {
+    for (int i = 0; i < nv; i += 2) {
         int e[2], j[2];
         float4 lv[2][KPAD / 4];
 #pragma unroll
@@ -899,7 +899,27 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                             }
                         }
                     }
-                    // An entry at or above the other half's k-th best of this row
+                    uint32_t seeded = 0u;   // bits of this pass already in ks
+                if (t == 0 && c == 0) {
+                    // seed the top-k with the pass's first K keys (the nearest tile):
+                    // a finite threshold from the start keeps the early tiles cheap
+                    float sk[K];
+                    int sj[K];
+#pragma unroll
+                    for (int i = 0; i < K; ++i) {
+                        const float sc = MODE == MODE_FOLD ? -2.f * key[i] : key[i];
+                        sk[i] = sc < 3.0e38f ? sc : 3.0e38f;   // padding (inf / NaN) sorts last
+                        sj[i] = jb + i;
+                    }
+                    bitonic_sort<K>(sk, sj);
+#pragma unroll
+                    for (int i = 0; i < K; ++i) { ks[i] = sk[i]; kj[i] = sj[i]; }
+                    thr = ks[K - 1];
+                    tthr = -0.5f * thr;
+                    S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                    seeded = K >= 32 ? 0xFFFFFFFFu : ((1u << K) - 1u);
+                }
+                // An entry at or above the other half's k-th best of this row
                     // cannot be in the row's overall top-k: filter with the tighter of
                     // the two (a stale read is only looser).
                     const uint2 pp = S.thr_pub[wg ^ 1][r];
@@ -919,7 +939,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                             for (int i = 0; i < w; ++i)
                                 ext[i] = MODE == MODE_FOLD ? fmaxf(ext[i], ext[i + w]) : fminf(ext[i], ext[i + w]);
                         const bool maybe = MODE == MODE_FOLD ? ext[0] > tthr_e : ext[0] < thr_e;
-                        if (!__any_sync(0xffffffffu, maybe)) continue;   // nothing for this warp here
+                        if (!__any_sync(0xffffffffu, maybe || seeded)) continue;   // nothing for this warp here
                     }
                     // eight independent 8-bit masks, then two 32-bit masks
                     uint32_t mk[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
@@ -928,7 +948,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                         const bool hit = MODE == MODE_FOLD ? key[i] > tthr_e : key[i] < thr_e;
                         if (hit) mk[i >> 3] |= 1u << (i & 7);
                     }
-                    uint32_t m0 = mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24);
+                    uint32_t m0 = (mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24)) & ~seeded;
                     uint32_t m1 = mk[4] | (mk[5] << 8) | (mk[6] << 16) | (mk[7] << 24);
                     const int nh0 = __popc(m0), nh1 = __popc(m1);
                     if (m0 | m1) {   // stage the keys for the append passes (lanes with hits only)
@@ -969,6 +989,15 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
             // every MMA of this voxel tile is complete: the next tile's A may go in now
             if (wg == 0 && lv + 1 < my_vt) write_voxel_tile<MODE>(S, P, vt + gridDim.x, r, lane);
             merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
+            S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+            // Candidates above the other half's k-th best cannot be in the row's
+            // overall top-k; ks is ascending, so the rest is a prefix of length nv
+            // (a stale partner value only keeps more).
+            const uint2 pp = S.thr_pub[wg ^ 1][r];
+            const float cut = fminf(3.0e38f, pp.x == (uint32_t)vt ? __uint_as_float(pp.y) : 3.0e38f);
+            int nv = 0;
+#pragma unroll
+            for (int i = 0; i < K; ++i) nv += (ks[i] < 3.0e38f && ks[i] <= cut) ? 1 : 0;
             // the (now empty) buffer carries the candidates to the rescore loop, so
             // ks/kj are only ever indexed by constants and stay in registers
 #pragma unroll
@@ -977,7 +1006,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
             const int64_t row = pos < P.n_vox ? P.vperm[pos] : -1;
             float best = 3.0e38f, bs0 = 0.f;
             int bj = 0x7FFFFFFF;
-            if (row >= 0) rescore<K, FREE>(P, row, mybuf, best, bj, bs0);
+            if (row >= 0) rescore<K, FREE>(P, row, mybuf, nv, best, bj, bs0);
             if (wg == 1) {
                 S.res1[lv & 1][r] = make_float4(best, __int_as_float(bj), bs0, 0.f);
                 __syncwarp();
