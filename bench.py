@@ -178,6 +178,8 @@ def main(argv=None):
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shape (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serving-requests", type=int, default=24)
     args = ap.parse_args(argv)
     ws, rank, local = _dist()
     if args.impl == "reference":
@@ -290,6 +292,8 @@ def main(argv=None):
                                 "sample": sample}
     if rank == 0 and ws == 1 and not args.no_secondary:
         line["secondary"] = secondary(dev)
+        if not args.no_serving:
+            line["secondary"]["serving"] = serving_run(dev, n_requests=args.serving_requests)
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
@@ -329,25 +333,89 @@ def secondary(dev):
     vox, truth = WL.rician_voxels(lib)
     L = torch.from_numpy(lib.astype(np.float32)).to(dev)
     M = torch.from_numpy(vox.astype(np.float32)).to(dev)
-    for prec in ("fp32", "bf16"):
-        try:
-            match_device(M[:4096], L, precision=prec)
-            torch.cuda.synchronize(dev)
+
+    def timed_match(Mx, Lx, prec, topk=32):
+        match_device(Mx[:4096], Lx, precision=prec, topk=topk)
+        torch.cuda.synchronize(dev)
+        best, idx = None, None
+        for _ in range(3):
             e0.record()
-            idx, _, _ = match_device(M, L, precision=prec)
+            idx, _, _ = match_device(Mx, Lx, precision=prec, topk=topk)
             e1.record()
             torch.cuda.synchronize(dev)
-            t = e0.elapsed_time(e1) / 1e3
-            out[f"match_{prec}_voxels_per_s"] = len(vox) / t
-            out[f"match_{prec}_ms"] = t * 1e3
-            out[f"match_{prec}_idx"] = idx
-        except Exception as exc:  # report, do not hide
-            out[f"match_{prec}_error"] = str(exc)[:200]
-    if "match_fp32_idx" in out and "match_bf16_idx" in out:
-        out["match_bf16_fp32_index_agreement"] = float((out["match_fp32_idx"] == out["match_bf16_idx"]).float().mean())
-    out.pop("match_fp32_idx", None)
-    out.pop("match_bf16_idx", None)
+            t = e0.elapsed_time(e1)
+            best = t if best is None else min(best, t)
+        return best, idx
+
+    match = {"library": [int(L.shape[0]), int(L.shape[1])], "voxels": int(M.shape[0]), "snr": 30}
+    try:
+        t32, i32 = timed_match(M, L, "fp32")
+        match["fp32_ms"] = t32
+        match["fp32_voxels_per_s"] = len(vox) / (t32 / 1e3)
+        for k in (32, 8):
+            tk, ik = timed_match(M, L, "bf16", k)
+            match[f"bf16_top{k}_ms"] = tk
+            match[f"bf16_top{k}_voxels_per_s"] = len(vox) / (tk / 1e3)
+            match[f"bf16_top{k}_speedup_vs_fp32"] = t32 / tk
+            match[f"bf16_top{k}_index_agreement_vs_fp32"] = float((ik == i32).float().mean())
+        # dense BF16 tensor work of the top-32 run: voxels x entries x K(=32, padded) x 2
+        flops = 2.0 * M.shape[0] * L.shape[0] * 32
+        match["bf16_top32_tensor_tflops"] = flops / (match["bf16_top32_ms"] / 1e3) / 1e12
+        cols = torch.as_tensor(WL.two_delta_columns(), device=dev)
+        M2, L2 = M[:, cols].contiguous(), L[:, cols].contiguous()
+        t2f, i2f = timed_match(M2, L2, "fp32")
+        t2b, i2b = timed_match(M2, L2, "bf16", 32)
+        match["two_delta"] = {"fp32_ms": t2f, "bf16_top32_ms": t2b, "speedup": t2f / t2b,
+                              "index_agreement": float((i2b == i2f).float().mean())}
+    except Exception as exc:  # report, do not hide
+        match["error"] = str(exc)[:200]
+    out["match"] = match
     return out
+
+
+def serving_run(dev, n_requests: int = 24) -> dict:
+    """Serving workload: Poisson arrivals at 50 req/s (seed 2), (kio, rho, V, cells)
+    triplets from the batched workload, walkers log-uniform in [1e4, 1e6], plus one
+    fit request (1e5 voxels, BF16 top-32) every eighth request; wall-clock p50/p99
+    latency (arrival -> result) and walker-steps/s."""
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300 import workloads as WL
+    from custom_madi_gb300.serving import FitRequest, Server, SimRequest, poisson_arrivals
+    from custom_madi_gb300.walker_gpu import kio_to_pp, pair_layout
+    cfg = WL.batch_config()
+    cols = S.build_columns(cfg)
+    lay = pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    trip = WL.batch_triplets(n_requests, seed=2)
+    t0 = time.perf_counter()
+    ens = WL.build_ensembles(trip, cfg, seed=200)
+    t_build = time.perf_counter() - t0
+    rng = np.random.default_rng(2)
+    walkers = np.exp(rng.uniform(np.log(1e4), np.log(1e6), n_requests)).astype(np.int64)
+    arrivals = poisson_arrivals(n_requests, 50.0, seed=2)
+    lib, _ = WL.match_library()
+    vox, _ = WL.rician_voxels(lib, n_vox=100_000, seed=5)
+    reqs = []
+    for i, ((kio, _rho, _V, _nc), e) in enumerate(zip(trip, ens)):
+        reqs.append(SimRequest(e, kio_to_pp(kio, e.mean_AV, cfg), 1000 + i, int(walkers[i]), float(arrivals[i])))
+        if i % 8 == 7:
+            reqs.append(FitRequest(vox.astype(np.float32), "bf16", 32, arrival=float(arrivals[i])))
+    srv = Server(cfg, lay, cfg.direction_array(), library=lib, device=dev)
+    for e in ens:
+        e.device(str(srv.dev))                      # geometry packed before the clock starts
+    out = srv.run(reqs, realtime=True)
+    sims = [r for r in out["records"] if r.kind == "sim"]
+    fits = [r for r in out["records"] if r.kind == "fit"]
+    return {"workload": "serving: Poisson 50 req/s, walkers log-uniform [1e4, 1e6], batched triplets, "
+                        "fit requests of 1e5 voxels",
+            "requests": len(reqs), "sim_requests": len(sims), "fit_requests": len(fits),
+            "p50_latency_s": out["p50_s"], "p99_latency_s": out["p99_s"],
+            "sim_p50_latency_s": float(np.percentile([r.latency for r in sims], 50)),
+            "fit_p50_latency_s": float(np.percentile([r.latency for r in fits], 50)) if fits else None,
+            "walker_steps_per_s": out["walker_steps_per_s"], "walker_steps": out["walker_steps"],
+            "span_s": out["span_s"], "launches": out["launches"],
+            "mixed_launch_fraction": float(np.mean([len(l) > 1 for l in srv.launch_log])) if srv.launch_log else 0.0,
+            "offered_walker_steps_per_s": float(walkers.sum() * cfg.n_steps / arrivals[-1]),
+            "host_ensemble_build_s": t_build}
 
 
 if __name__ == "__main__":

@@ -409,6 +409,12 @@ class DeviceGeometry:
         self.struct = s
         self.stage_bytes = len(blob)
 
+    @property
+    def nbytes(self) -> int:
+        """Device bytes held by this geometry (stage blob, fp64 seeds, KD arrays)."""
+        ts = [self.stage, self.seed_f64, *self.kd]
+        return int(sum(t.numel() * t.element_size() for t in ts))
+
 
 # ---------------------------------------------------------------------------
 # Construction

@@ -253,7 +253,12 @@ class WalkBatch:
     def __init__(self, jobs: Sequence[WalkJob], cfg: SimConfig, *, layout: Optional[PairLayout] = None,
                  dirs: Optional[np.ndarray] = None, out_mode: int = N.MADI_OUT_FUSED,
                  stream: Optional[WalkRandomStream] = None, precision: int = 32,
-                 launch: Optional[LaunchConfig] = None, device=None):
+                 launch: Optional[LaunchConfig] = None, device=None,
+                 outputs: Optional[Tuple] = None, slots: Optional[Sequence[int]] = None):
+        """``outputs`` = (accum, occupancy, counters) pools owned by the caller and
+        ``slots`` the pool row of each job: the walk then adds into those rows
+        and never zeroes them (the sums are exact integers, so a job split over
+        several launches adds up to the same values as one launch)."""
         if not jobs:
             raise ValueError("a walk batch needs at least one job")
         self.dev = torch.device(device or "cuda")
@@ -284,8 +289,9 @@ class WalkBatch:
             pp = _checked_pp(j.pp)
             t1, t2 = _thresholds(pp)
             nt = (int(j.n_walkers) + tw - 1) // tw
+            slot = s if slots is None else int(slots[s])
             jb = N.MadiWalkJob(gidx[id(j.ensemble)], int(j.n_walkers), int(j.walker_base) & 0xFFFFFFFF,
-                               int(j.walk_seed) & 0xFFFFFFFF, PHILOX_KEY1, s, tiles, rows, pp, t1, t2)
+                               int(j.walk_seed) & 0xFFFFFFFF, PHILOX_KEY1, slot, tiles, rows, pp, t1, t2)
             jbytes.append(bytes(jb))
             tiles += nt
             rows += int(j.n_walkers)
@@ -318,7 +324,8 @@ class WalkBatch:
                 for a in range(3):
                     d.dirs[3 * k + a] = float(u[k, a])
             self.n_out = layout.n_pairs * layout.n_b * len(u)
-            self.accum = torch.zeros((n_slots, self.n_out * 2), dtype=torch.int64, device=self.dev)
+            if outputs is None:
+                self.accum = torch.zeros((n_slots, self.n_out * 2), dtype=torch.int64, device=self.dev)
         else:
             d.n_pairs, d.n_b, d.n_dirs = 0, 0, 0
             self.n_out = 0
@@ -326,8 +333,18 @@ class WalkBatch:
             self.Y = torch.zeros((rows, cfg.n_grid, 3), dtype=torch.float64, device=self.dev)
             self.inside_trace = torch.zeros((rows, cfg.n_grid), dtype=torch.int8, device=self.dev)
             d.Y, d.inside_trace = N.ptr(self.Y), N.ptr(self.inside_trace)
-        self.occupancy = torch.zeros((n_slots, cfg.n_grid), dtype=torch.int64, device=self.dev)
-        self.counters = torch.zeros((n_slots, N.MADI_CNT_N), dtype=torch.int64, device=self.dev)
+        self.owns_outputs = outputs is None
+        if outputs is None:
+            self.occupancy = torch.zeros((n_slots, cfg.n_grid), dtype=torch.int64, device=self.dev)
+            self.counters = torch.zeros((n_slots, N.MADI_CNT_N), dtype=torch.int64, device=self.dev)
+        else:
+            if out_mode != N.MADI_OUT_FUSED or slots is None or len(slots) != len(self.jobs):
+                raise ValueError("external output pools need the fused epilogue and one slot per job")
+            self.accum, self.occupancy, self.counters = outputs
+            if self.accum.shape[1] != self.n_out * 2 or self.occupancy.shape[1] != cfg.n_grid:
+                raise ValueError("output pool shapes do not match the layout / grid")
+            if max(slots) >= self.accum.shape[0]:
+                raise ValueError("slot outside the output pool")
         self.work_counter = torch.zeros(4, dtype=torch.int32, device=self.dev)
         d.accum, d.occupancy, d.counters = N.ptr(self.accum), N.ptr(self.occupancy), N.ptr(self.counters)
         d.work_counter = N.ptr(self.work_counter)
@@ -360,9 +377,10 @@ class WalkBatch:
         s = stream if stream is not None else torch.cuda.current_stream(self.dev)
         with torch.cuda.stream(s):
             self.work_counter.zero_()
-            self.accum.zero_()
-            self.occupancy.zero_()
-            self.counters.zero_()
+            if self.owns_outputs:
+                self.accum.zero_()
+                self.occupancy.zero_()
+                self.counters.zero_()
         st = N.lib().madi_walk(C.byref(self.desc), s.cuda_stream)
         N.check(st, "madi_walk")
 
