@@ -44,7 +44,13 @@ EXPORTED = (
     "madi_abi_version", "madi_last_error_string", "madi_classify", "madi_walk",
     "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_scratch_bytes",
     "madi_kdtree_build", "madi_grid_build", "madi_walk_blocks_per_sm", "madi_walk_noalloc",
+    "madi_walk_batched", "madi_autotune_load", "madi_autotune_store",
 )
+
+
+class MadiLaunchShape(C.Structure):
+    _fields_ = [("tile_walkers", C.c_int32), ("blocks_per_sm", C.c_int32), ("min_blocks", C.c_int32),
+                ("stage_budget", C.c_int32), ("walker_steps_per_s", C.c_double)]
 
 
 class MadiGeometry(C.Structure):
@@ -118,6 +124,9 @@ def _declare(lib):
     lib.madi_classify.argtypes = [C.POINTER(MadiGeometry), P, C.c_int, C.c_int64, C.c_int, P, P, P, P]
     lib.madi_walk.argtypes = [C.POINTER(MadiWalkDesc), P]
     lib.madi_walk_noalloc.argtypes = [C.POINTER(MadiWalkDesc), P]
+    lib.madi_walk_batched.argtypes = [C.POINTER(MadiWalkDesc), P]
+    lib.madi_autotune_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(MadiLaunchShape)]
+    lib.madi_autotune_store.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(MadiLaunchShape)]
     lib.madi_walk_smem_bytes.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     lib.madi_walk_smem_bytes.restype = C.c_int64
     lib.madi_walk_blocks_per_sm.argtypes = [C.POINTER(MadiWalkDesc)]
@@ -129,8 +138,9 @@ def _declare(lib):
     lib.madi_kdtree_build.argtypes = [P, C.c_int32, P, P, P, P, P]
     lib.madi_grid_build.argtypes = [P, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
                                     P, P, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
-    for name in ("madi_classify", "madi_walk", "madi_walk_noalloc", "madi_reduce_Y", "madi_match",
-                 "madi_kdtree_build", "madi_grid_build"):
+    for name in ("madi_classify", "madi_walk", "madi_walk_noalloc", "madi_walk_batched", "madi_reduce_Y",
+                 "madi_match", "madi_kdtree_build", "madi_grid_build", "madi_autotune_load",
+                 "madi_autotune_store"):
         getattr(lib, name).restype = C.c_int
 
 

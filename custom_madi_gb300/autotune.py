@@ -1,17 +1,18 @@
 """Launch-shape autotuner for the batched walker.
 
-For a batch it times the candidate (tile_walkers, blocks_per_sm) shapes on a
-representative sub-batch (the first jobs, enough tiles to fill every SM a few
-times, full walk length) with CUDA events and keeps the fastest.  Winners are
-cached in a JSON file keyed by (SM count, cell-count bucket of the largest
-ensemble, output columns x directions, staged-or-not), so a repeated build
-pays nothing.  The cache path is $MADI_AUTOTUNE_CACHE or
-~/.cache/custom_madi_gb300/autotune.json.
+For a batch it times the candidate (tile_walkers, blocks_per_sm, register
+budget, stage budget) shapes on a representative sub-batch (the first jobs,
+enough tiles to fill every SM a few times, full walk length) with CUDA events
+and keeps the fastest.  Winners are stored by the native cache
+(``madi_autotune_load`` / ``madi_autotune_store``) keyed by (SM count, seed-count
+bucket of the largest ensemble, stage-size bucket, output columns x
+directions), so a repeated build pays nothing.  The cache file is
+$MADI_AUTOTUNE_CACHE or ~/.cache/custom_madi_gb300/autotune.tsv.
 """
 
 from __future__ import annotations
 
-import json
+import ctypes as C
 import os
 import threading
 from pathlib import Path
@@ -19,6 +20,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
+from . import _native as N
 from .walker_gpu import LaunchConfig, PairLayout, WalkBatch, WalkJob
 
 # (tile_walkers, blocks_per_sm (0 = occupancy), min_blocks register budget, stage budget bytes)
@@ -29,26 +31,21 @@ _lock = threading.Lock()
 
 def cache_path() -> Path:
     p = os.environ.get("MADI_AUTOTUNE_CACHE")
-    return Path(p) if p else Path.home() / ".cache" / "custom_madi_gb300" / "autotune.json"
+    return Path(p) if p else Path.home() / ".cache" / "custom_madi_gb300" / "autotune.tsv"
 
 
-def load() -> dict:
-    p = cache_path()
-    try:
-        return json.loads(p.read_text())
-    except (OSError, ValueError):
-        return {}
+def load(key: str) -> Optional[N.MadiLaunchShape]:
+    """Stored shape for ``key`` or None."""
+    sh = N.MadiLaunchShape()
+    st = N.lib().madi_autotune_load(str(cache_path()).encode(), key.encode(), C.byref(sh))
+    N.check(st, "madi_autotune_load")
+    return sh if sh.tile_walkers > 0 else None
 
 
-def store(table: dict) -> None:
-    p = cache_path()
-    try:
-        p.parent.mkdir(parents=True, exist_ok=True)
-        tmp = p.with_suffix(".tmp")
-        tmp.write_text(json.dumps(table, indent=1, sort_keys=True))
-        os.replace(tmp, p)
-    except OSError:
-        pass
+def store(key: str, tile_walkers: int, blocks_per_sm: int, min_blocks: int, stage_budget: int, rate: float) -> bool:
+    sh = N.MadiLaunchShape(int(tile_walkers), int(blocks_per_sm), int(min_blocks), int(stage_budget), float(rate))
+    st = N.lib().madi_autotune_store(str(cache_path()).encode(), key.encode(), C.byref(sh))
+    return st == 0     # an unwritable cache only costs a re-tune next time
 
 
 def key_for(jobs: Sequence[WalkJob], layout: PairLayout, n_dirs: int, sm_count: int) -> str:
@@ -87,12 +84,11 @@ def choose(jobs: Sequence[WalkJob], cfg, layout: PairLayout, dirs, device=None, 
     n_dirs = len(dirs)
     key = key_for(jobs, layout, n_dirs, sm)
     with _lock:
-        table = load()
-    if not retune and key in table and "min_blocks" in table[key]:
-        e = table[key]
-        return LaunchConfig(tile_walkers=int(e["tile_walkers"]), blocks_per_sm=int(e["blocks_per_sm"]),
-                            min_blocks=int(e["min_blocks"]), stage_budget=int(e["stage_budget"]),
-                            staged=bool(e["stage_budget"]))
+        e = None if retune else load(key)
+    if e is not None:
+        return LaunchConfig(tile_walkers=int(e.tile_walkers), blocks_per_sm=int(e.blocks_per_sm),
+                            min_blocks=int(e.min_blocks), stage_budget=int(e.stage_budget),
+                            staged=bool(e.stage_budget))
     target = budget_tiles or sm * 8
     sub, tiles = [], 0
     for j in jobs:
@@ -113,9 +109,5 @@ def choose(jobs: Sequence[WalkJob], cfg, layout: PairLayout, dirs, device=None, 
         return LaunchConfig()
     (tw, bps, mb, sb), rate = max(results.items(), key=lambda kv: kv[1])
     with _lock:
-        table = load()
-        table[key] = {"tile_walkers": tw, "blocks_per_sm": bps, "min_blocks": mb, "stage_budget": sb,
-                      "walker_steps_per_s": rate,
-                      "tried": {"x".join(map(str, c)): r for c, r in results.items()}}
-        store(table)
+        store(key, tw, bps, mb, sb, rate)
     return LaunchConfig(tile_walkers=tw, blocks_per_sm=bps, min_blocks=mb, stage_budget=sb, staged=bool(sb))

@@ -8,6 +8,11 @@
 #include <cstring>
 #include <numeric>
 #include <vector>
+#include <filesystem>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
 #include "madi_host.h"
 
 namespace madi {
@@ -226,5 +231,75 @@ extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G
     if (count > 0xFFFFFFFFll) return host::fail(MADI_ERR_CAPACITY, "grid_build: more than 2^32 candidate ids");
     if (ids && count > capacity) return host::fail(MADI_ERR_CAPACITY, "grid_build: capacity %lld < %lld ids",
                                                    (long long)capacity, (long long)count);
+    return MADI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner cache: one "key\ttile\tbps\tminb\tstage\trate" line per key.
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_tune_mu;
+
+bool valid_key(const char* key) {
+    if (!key || !*key) return false;
+    for (const char* c = key; *c; ++c)
+        if (*c == '\t' || *c == '\n' || *c == '\r') return false;
+    return true;
+}
+
+bool parse_line(const std::string& line, std::string& key, madi_launch_shape& sh) {
+    std::istringstream in(line);
+    if (!std::getline(in, key, '\t') || key.empty()) return false;
+    return static_cast<bool>(in >> sh.tile_walkers >> sh.blocks_per_sm >> sh.min_blocks >> sh.stage_budget >>
+                             sh.walker_steps_per_s);
+}
+}  // namespace
+
+extern "C" madi_status madi_autotune_load(const char* path, const char* key, madi_launch_shape* out) {
+    host::clear_error();
+    if (!path || !out || !valid_key(key)) return host::fail(MADI_ERR_INVALID, "autotune_load: bad arguments");
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    *out = madi_launch_shape{};
+    std::ifstream f(path);
+    if (!f) return MADI_OK;
+    std::string line, k;
+    while (std::getline(f, line)) {
+        madi_launch_shape sh{};
+        if (parse_line(line, k, sh) && k == key) *out = sh;   // last entry wins
+    }
+    return MADI_OK;
+}
+
+extern "C" madi_status madi_autotune_store(const char* path, const char* key, const madi_launch_shape* shape) {
+    host::clear_error();
+    if (!path || !shape || !valid_key(key) || shape->tile_walkers <= 0)
+        return host::fail(MADI_ERR_INVALID, "autotune_store: bad arguments");
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    std::vector<std::string> keep;
+    {
+        std::ifstream f(path);
+        std::string line, k;
+        while (f && std::getline(f, line)) {
+            madi_launch_shape sh{};
+            if (parse_line(line, k, sh) && k != key) keep.push_back(line);
+        }
+    }
+    std::ostringstream row;
+    row.precision(17);
+    row << key << '\t' << shape->tile_walkers << '\t' << shape->blocks_per_sm << '\t' << shape->min_blocks << '\t'
+        << shape->stage_budget << '\t' << shape->walker_steps_per_s;
+    keep.push_back(row.str());
+    std::error_code ec;
+    const std::filesystem::path p(path);
+    if (p.has_parent_path()) std::filesystem::create_directories(p.parent_path(), ec);
+    const std::string tmp = std::string(path) + ".tmp";
+    {
+        std::ofstream o(tmp, std::ios::trunc);
+        if (!o) return host::fail(MADI_ERR_INVALID, "autotune_store: cannot write %s", tmp.c_str());
+        for (const auto& l : keep) o << l << '\n';
+        if (!o) return host::fail(MADI_ERR_INVALID, "autotune_store: write failed for %s", tmp.c_str());
+    }
+    std::filesystem::rename(tmp, p, ec);
+    if (ec) return host::fail(MADI_ERR_INVALID, "autotune_store: rename to %s failed", path);
     return MADI_OK;
 }

@@ -745,6 +745,22 @@ madi_status static_scratch(uint32_t** out) {
 }
 }  // namespace
 
+extern "C" madi_status madi_walk_batched(const madi_walk_desc* desc, void* stream) {
+    host::clear_error();
+    if (!desc) return host::fail(MADI_ERR_INVALID, "walk_batched: null descriptor");
+    if (desc->precision != 32) return host::fail(MADI_ERR_INVALID, "walk_batched: fp32 walkers only");
+    madi_walk_desc d = *desc;
+    if (d.grid_blocks <= 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int32_t bps = madi_walk_blocks_per_sm(&d);
+        if (bps <= 0) return host::fail(MADI_ERR_CUDA, "walk_batched: no resident block fits this descriptor");
+        d.grid_blocks = (int32_t)std::min<int64_t>((int64_t)sms * bps, std::max<int64_t>(d.n_tiles, 1));
+    }
+    return madi_walk(&d, stream);
+}
+
 extern "C" madi_status madi_walk_noalloc(const madi_walk_desc* desc, void* stream) {
     host::clear_error();
     if (!desc) return host::fail(MADI_ERR_INVALID, "null walk descriptor");

@@ -212,6 +212,12 @@ int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walkers, int32_t 
  * (tile_walkers threads, stage_smem + epilogue shared memory); 0 on error. */
 int32_t madi_walk_blocks_per_sm(const madi_walk_desc* desc);
 
+/* The batched (persistent, work-queue) walk: madi_walk with a persistent grid.
+ * grid_blocks == 0 means SMs x madi_walk_blocks_per_sm(desc).  Replaces the
+ * per-ensemble launches of _run_walk_one_ensemble (madi/walker_gpu.py:843-953)
+ * driven from the ensemble x kio loop (:1218-1232). */
+madi_status madi_walk_batched(const madi_walk_desc* desc, void* stream);
+
 /* Replaces _reduce_kernel (madi/walker_gpu.py:658-695) for grids too large for
  * the fused epilogue: Y [n_walkers][n_grid][3] fp64 -> cos_sum / sin_sum
  * [n_cols] fp64 over the 3 axes, columns (jd, jD, js, coef). */
@@ -280,6 +286,26 @@ madi_status madi_kdtree_build(const double* seeds_xyz, int32_t n, int32_t* node_
 madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h,
                             double eps, double safe_cap, uint32_t* offsets,
                             void* ids, int32_t ids_u32, int64_t capacity, int64_t* total);
+
+/* ------------------------------------------------------------------------ */
+/* Autotuner cache (no counterpart in the reference)                        */
+/* ------------------------------------------------------------------------ */
+
+/* Launch shape of the batched walk chosen for one workload class. */
+typedef struct madi_launch_shape {
+    int32_t tile_walkers;          /* 0: no entry for the key        */
+    int32_t blocks_per_sm;         /* 0: occupancy-derived           */
+    int32_t min_blocks;            /* register budget (1 or 2)       */
+    int32_t stage_budget;          /* bytes; 0: geometry read in place */
+    double  walker_steps_per_s;    /* rate measured when stored      */
+} madi_launch_shape;
+
+/* Text file of "key<TAB>tile<TAB>bps<TAB>minb<TAB>stage<TAB>rate" lines; keys hold
+ * no tab or newline.  load: an absent file or key gives tile_walkers = 0.
+ * store: replaces or appends the key, written to path.tmp then renamed (the
+ * parent directory is created).  Thread-safe within a process. */
+madi_status madi_autotune_load(const char* path, const char* key, madi_launch_shape* out);
+madi_status madi_autotune_store(const char* path, const char* key, const madi_launch_shape* shape);
 
 /* ------------------------------------------------------------------------ */
 /* Misc                                                                     */

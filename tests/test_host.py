@@ -32,7 +32,8 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layout_matches_header(tmp_path):
     """ctypes mirrors == the C compiler's layout of the header structs."""
     structs = {"madi_geometry": N.MadiGeometry, "madi_walk_job": N.MadiWalkJob,
-               "madi_walk_desc": N.MadiWalkDesc, "madi_match_desc": N.MadiMatchDesc}
+               "madi_walk_desc": N.MadiWalkDesc, "madi_match_desc": N.MadiMatchDesc,
+               "madi_launch_shape": N.MadiLaunchShape}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/madi_gb300.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
@@ -178,3 +179,31 @@ def test_pair_layout_and_thresholds():
     m = W._membrane_transition_counts([1, 1, 1, 1, 1], [True, False, True, True, False], [1, 1, 2, 1, 1],
                                       [False, True, True, True, False])
     assert m.tolist() == [1, 1, 2, 0, 0]
+
+
+def test_autotune_cache_store_load_roundtrip(tmp_path):
+    """Native launch-shape cache: absent -> empty, store / replace / reload, bad keys rejected."""
+    import ctypes as C
+    from custom_madi_gb300 import _native as N
+    path = str(tmp_path / "sub" / "tune.tsv").encode()
+    sh = N.MadiLaunchShape()
+    assert N.lib().madi_autotune_load(path, b"sm152/seeds512", C.byref(sh)) == 0 and sh.tile_walkers == 0
+    for key, tw in ((b"sm152/seeds512", 128), (b"sm152/seeds1024", 256), (b"sm152/seeds512", 64)):
+        st = N.lib().madi_autotune_store(path, key, C.byref(N.MadiLaunchShape(tw, 0, 2, 49152, 6.4e9)))
+        assert st == 0, N.lib().madi_last_error_string()
+    assert N.lib().madi_autotune_load(path, b"sm152/seeds512", C.byref(sh)) == 0
+    assert (sh.tile_walkers, sh.blocks_per_sm, sh.min_blocks, sh.stage_budget) == (64, 0, 2, 49152)
+    assert sh.walker_steps_per_s == 6.4e9
+    assert N.lib().madi_autotune_load(path, b"sm152/seeds1024", C.byref(sh)) == 0 and sh.tile_walkers == 256
+    lines = (tmp_path / "sub" / "tune.tsv").read_text().splitlines()
+    assert len(lines) == 2
+    assert N.lib().madi_autotune_store(path, b"bad\tkey", C.byref(N.MadiLaunchShape(1, 0, 1, 0, 1.0))) == N.MADI_ERR_INVALID
+
+
+def test_autotune_python_cache_uses_native_store(tmp_path, monkeypatch):
+    from custom_madi_gb300 import autotune
+    monkeypatch.setenv("MADI_AUTOTUNE_CACHE", str(tmp_path / "t.tsv"))
+    assert autotune.load("k1") is None
+    assert autotune.store("k1", 256, 0, 1, 0, 5.0e9)
+    e = autotune.load("k1")
+    assert (e.tile_walkers, e.min_blocks) == (256, 1)
