@@ -22,7 +22,7 @@ OBJDIR = LIBDIR / "obj"
 LIBNAME = "libmadi_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["walk.cu", "classify.cu", "match.cu", "match_bf16.cu"]
-CPP_SOURCES = ["host.cpp"]
+CPP_SOURCES = ["host.cpp", "serve.cpp"]
 
 
 def nvcc_path() -> str:

@@ -45,6 +45,8 @@ EXPORTED = (
     "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_scratch_bytes",
     "madi_kdtree_build", "madi_grid_build", "madi_walk_blocks_per_sm", "madi_walk_noalloc",
     "madi_walk_batched", "madi_autotune_load", "madi_autotune_store",
+    "madi_serve_arena_bytes", "madi_serve_create", "madi_serve_submit", "madi_serve_poll",
+    "madi_serve_release", "madi_serve_destroy",
 )
 
 
@@ -107,6 +109,22 @@ class MadiMatchDesc(C.Structure):
     ]
 
 
+class MadiServeConfig(C.Structure):
+    _fields_ = [("walk", MadiWalkDesc), ("n_slots", C.c_int32), ("chunk_walkers", C.c_int32),
+                ("launch_walkers", C.c_int32), ("inflight", C.c_int32), ("budget_bytes", C.c_int64),
+                ("arena", C.c_void_p), ("arena_bytes", C.c_int64)]
+
+
+class MadiServeRequest(C.Structure):
+    _fields_ = [("geometry", MadiGeometry), ("pp", C.c_double), ("seed", C.c_uint32), ("pad0", C.c_uint32),
+                ("n_walkers", C.c_int64), ("nbytes", C.c_int64)]
+
+
+class MadiServeDone(C.Structure):
+    _fields_ = [("request_id", C.c_int64), ("slot", C.c_int32), ("pad0", C.c_int32),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double)]
+
+
 class MadiError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(message)
@@ -127,6 +145,14 @@ def _declare(lib):
     lib.madi_walk_batched.argtypes = [C.POINTER(MadiWalkDesc), P]
     lib.madi_autotune_load.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(MadiLaunchShape)]
     lib.madi_autotune_store.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(MadiLaunchShape)]
+    lib.madi_serve_arena_bytes.argtypes = [C.POINTER(MadiServeConfig)]
+    lib.madi_serve_arena_bytes.restype = C.c_int64
+    lib.madi_serve_create.argtypes = [C.POINTER(MadiServeConfig), C.POINTER(C.c_void_p)]
+    lib.madi_serve_submit.argtypes = [P, C.POINTER(MadiServeRequest), C.POINTER(C.c_int64)]
+    lib.madi_serve_poll.argtypes = [P, C.c_int32, C.POINTER(MadiServeDone), C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32)]
+    lib.madi_serve_release.argtypes = [P, C.c_int64]
+    lib.madi_serve_destroy.argtypes = [P]
     lib.madi_walk_smem_bytes.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     lib.madi_walk_smem_bytes.restype = C.c_int64
     lib.madi_walk_blocks_per_sm.argtypes = [C.POINTER(MadiWalkDesc)]
@@ -140,7 +166,8 @@ def _declare(lib):
                                     P, P, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
     for name in ("madi_classify", "madi_walk", "madi_walk_noalloc", "madi_walk_batched", "madi_reduce_Y",
                  "madi_match", "madi_kdtree_build", "madi_grid_build", "madi_autotune_load",
-                 "madi_autotune_store"):
+                 "madi_autotune_store", "madi_serve_create", "madi_serve_submit", "madi_serve_poll",
+                 "madi_serve_release", "madi_serve_destroy"):
         getattr(lib, name).restype = C.c_int
 
 

@@ -333,6 +333,138 @@ class Server:
                 "walker_steps_per_s": steps / span if span > 0 else float("nan")}
 
 
+def _walk_template(cfg: SimConfig, layout: PairLayout, dirs: np.ndarray, boundary: int,
+                   lc: LaunchConfig) -> "N.MadiWalkDesc":
+    """The job-independent part of a fused fp32 Philox walk descriptor."""
+    d = N.MadiWalkDesc()
+    d.tile_walkers = int(lc.tile_walkers)
+    d.boundary = int(boundary)
+    d.precision = 32
+    d.rng = N.MADI_RNG_PHILOX
+    d.out_mode = N.MADI_OUT_FUSED
+    d.n_steps, d.steps_per_h, d.n_grid = cfg.n_steps, cfg.steps_per_h, cfg.n_grid
+    d.sigma, d.ts = cfg.sigma, cfg.ts
+    d.min_blocks = int(lc.min_blocks)
+    d.n_pairs, d.n_b, d.n_dirs = layout.n_pairs, layout.n_b, len(dirs)
+    for p in range(layout.n_pairs):
+        d.pair_jd[p], d.pair_jD[p], d.pair_js[p] = int(layout.jd[p]), int(layout.jD[p]), int(layout.js[p])
+        for b in range(layout.n_b):
+            d.coef[p * layout.n_b + b] = float(layout.coef[p, b])
+    for k in range(len(dirs)):
+        for a in range(3):
+            d.dirs[3 * k + a] = float(dirs[k, a])
+    d.stage_smem = 0                       # geometry read in place
+    return d
+
+
+class NativeSimServer:
+    """Simulation requests served by the native loop (``madi_serve_*``): the same
+    admission and chunking rules as ``Server``, run by the C++ runtime; results
+    are read from the slot pools.  Periodic or fatal-escape geometries, one kind
+    per server."""
+
+    def __init__(self, cfg: SimConfig, layout: PairLayout, dirs: np.ndarray, *, boundary: int,
+                 budget_bytes: int = 8 << 30, n_slots: int = 64, chunk_walkers: int = 65536,
+                 launch_walkers: int = 155648, inflight: int = 2, launch: Optional[LaunchConfig] = None,
+                 device=None):
+        import ctypes as C
+        if torch is None or not torch.cuda.is_available():
+            raise RuntimeError("the server runs on a CUDA device")
+        self.dev = torch.device(device or "cuda")
+        self.cfg, self.layout = cfg, layout
+        self.dirs = np.asarray(dirs, np.float64)
+        self.n_out = layout.n_pairs * layout.n_b * len(self.dirs)
+        lc = launch or LaunchConfig()
+        self.accum = torch.zeros((n_slots, self.n_out * 2), dtype=torch.int64, device=self.dev)
+        self.occupancy = torch.zeros((n_slots, cfg.n_grid), dtype=torch.int64, device=self.dev)
+        self.counters = torch.zeros((n_slots, N.MADI_CNT_N), dtype=torch.int64, device=self.dev)
+        sc = N.MadiServeConfig()
+        sc.walk = _walk_template(cfg, layout, self.dirs, boundary, lc)
+        sc.walk.accum, sc.walk.occupancy, sc.walk.counters = N.ptr(self.accum), N.ptr(self.occupancy), N.ptr(self.counters)
+        sc.n_slots, sc.chunk_walkers, sc.launch_walkers, sc.inflight = n_slots, chunk_walkers, launch_walkers, inflight
+        sc.budget_bytes = int(budget_bytes)
+        need = int(N.lib().madi_serve_arena_bytes(C.byref(sc)))
+        self.arena = torch.empty(need + 256, dtype=torch.uint8, device=self.dev)
+        base = N.ptr(self.arena)
+        sc.arena, sc.arena_bytes = base + ((-base) % 256), need
+        self._cfg_struct = sc
+        h = C.c_void_p()
+        N.check(N.lib().madi_serve_create(C.byref(sc), C.byref(h)), "madi_serve_create")
+        self._h = h
+        self._C = C
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().madi_serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _result(self, slot: int) -> dict:
+        lay = self.layout
+        a = self.accum[slot].cpu().numpy().reshape(lay.n_pairs, lay.n_b, len(self.dirs), 2)
+        n_cols = int(lay.col_of.max()) + 1
+        cs = np.zeros((n_cols, len(self.dirs)), np.int64)
+        ss = np.zeros((n_cols, len(self.dirs)), np.int64)
+        for p in range(lay.n_pairs):
+            for b in range(lay.n_b):
+                c = lay.col_of[p, b]
+                if c >= 0:
+                    cs[c], ss[c] = a[p, b, :, 0], a[p, b, :, 1]
+        return {"cos_fixed": cs, "sin_fixed": ss, "cos": cs / FIXED_POINT_SCALE, "sin": ss / FIXED_POINT_SCALE,
+                "occupancy": self.occupancy[slot].cpu().numpy(),
+                "counters": dict(zip(N.CNT_NAMES, self.counters[slot].cpu().numpy().tolist()))}
+
+    def run(self, requests: Sequence[SimRequest], *, realtime: bool = True, poll_s: float = 2e-4) -> Dict[str, Any]:
+        C = self._C
+        torch.cuda.synchronize(self.dev)       # pools and geometry ready before the native streams start
+        order = sorted(range(len(requests)), key=lambda i: requests[i].arrival)
+        recs = {i: Record(i, "sim", float(requests[i].arrival),
+                          requests[i].ensemble.device(str(self.dev)).nbytes) for i in order}
+        for i in order:
+            recs[i].walker_steps = int(requests[i].n_walkers) * self.cfg.n_steps
+        pending, ids = list(order), {}
+        done = (N.MadiServeDone * 64)()
+        n_done, n_pend = C.c_int32(), C.c_int32()
+        t0 = time.perf_counter()
+        remaining = len(order)
+        while remaining:
+            t = time.perf_counter() - t0
+            while pending and (not realtime or requests[pending[0]].arrival <= t):
+                i = pending.pop(0)
+                r = requests[i]
+                q = N.MadiServeRequest()
+                q.geometry = r.ensemble.device(str(self.dev)).struct
+                q.pp, q.seed, q.n_walkers, q.nbytes = float(r.pp), int(r.seed) & 0xFFFFFFFF, int(r.n_walkers), recs[i].nbytes
+                rid = C.c_int64()
+                N.check(N.lib().madi_serve_submit(self._h, C.byref(q), C.byref(rid)), "madi_serve_submit")
+                ids[rid.value] = i
+                recs[i].admit = None
+            N.check(N.lib().madi_serve_poll(self._h, 64, done, C.byref(n_done), C.byref(n_pend)), "madi_serve_poll")
+            for k in range(n_done.value):
+                d = done[k]
+                i = ids[d.request_id]
+                r = recs[i]
+                r.slot = d.slot
+                r.admit = r.arrival + (d.admit_s - d.submit_s)
+                r.finish = time.perf_counter() - t0
+                r.result = self._result(d.slot)
+                N.check(N.lib().madi_serve_release(self._h, d.request_id), "madi_serve_release")
+                remaining -= 1
+            if remaining and n_done.value == 0:
+                time.sleep(poll_s)
+        recs_l = [recs[i] for i in order]
+        lat = np.array([r.latency for r in recs_l])
+        span = max(r.finish for r in recs_l) - min(r.arrival for r in recs_l)
+        steps = sum(r.walker_steps for r in recs_l)
+        return {"records": recs_l, "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "walker_steps": steps, "span_s": span, "walker_steps_per_s": steps / span if span > 0 else float("nan")}
+
+
 def to_reduced(rec: Record, req: SimRequest, cfg: SimConfig):
     """A finished simulation record as the reference's ReducedResult."""
     from .walker_gpu import results_to_reduced

@@ -288,6 +288,58 @@ madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h,
                             void* ids, int32_t ids_u32, int64_t capacity, int64_t* total);
 
 /* ------------------------------------------------------------------------ */
+/* Serving loop (no counterpart in the reference)                           */
+/* ------------------------------------------------------------------------ */
+
+/* Continuous batching of simulation requests over madi_walk.  Requests are
+ * admitted in submission order while their declared device bytes fit the
+ * budget and an output slot is free; active requests are cut into
+ * tile-aligned walker chunks and every launch takes the next chunk of each
+ * active request (round robin, up to launch_walkers), up to `inflight`
+ * launches on server-owned streams.  A request's sums land in its slot row of
+ * the pools given in `walk` (accum/occupancy/counters) and are bit-identical
+ * however it was chunked or mixed.  Not thread-safe across servers sharing
+ * pools; calls on one server are serialised internally. */
+typedef struct madi_serve_config {
+    madi_walk_desc walk;           /* template: fused Philox walk; geoms/jobs/n_* /grid_blocks/work_counter
+                                      are the server's, accum/occupancy/counters = [n_slots] pools */
+    int32_t n_slots;
+    int32_t chunk_walkers;         /* multiple of walk.tile_walkers */
+    int32_t launch_walkers;        /* >= chunk_walkers */
+    int32_t inflight;              /* 1..4 launches in flight */
+    int64_t budget_bytes;          /* device bytes admitted requests may hold together */
+    void*   arena;                 /* device, 256-byte aligned, madi_serve_arena_bytes() bytes */
+    int64_t arena_bytes;
+} madi_serve_config;
+
+typedef struct madi_serve_request {
+    madi_geometry geometry;        /* device pointers valid until the request is released */
+    double   pp;
+    uint32_t seed;                 /* Philox key word 0 */
+    uint32_t pad0;
+    int64_t  n_walkers;
+    int64_t  nbytes;               /* device bytes the request holds while admitted */
+} madi_serve_request;
+
+typedef struct madi_serve_done {
+    int64_t request_id;
+    int32_t slot;                  /* row of the pools holding the result */
+    int32_t pad0;
+    double  submit_s, admit_s, finish_s;   /* seconds since madi_serve_create */
+} madi_serve_done;
+
+int64_t madi_serve_arena_bytes(const madi_serve_config* cfg);
+madi_status madi_serve_create(const madi_serve_config* cfg, void** server);
+madi_status madi_serve_submit(void* server, const madi_serve_request* req, int64_t* request_id);
+/* Non-blocking: admits, launches, reaps finished launches; reports up to
+ * max_done finished requests (each once) and the number still queued or active. */
+madi_status madi_serve_poll(void* server, int32_t max_done, madi_serve_done* done, int32_t* n_done,
+                            int32_t* n_pending);
+/* The caller has read request_id's slot: its slot and bytes return to the pool. */
+madi_status madi_serve_release(void* server, int64_t request_id);
+madi_status madi_serve_destroy(void* server);
+
+/* ------------------------------------------------------------------------ */
 /* Autotuner cache (no counterpart in the reference)                        */
 /* ------------------------------------------------------------------------ */
 

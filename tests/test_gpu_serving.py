@@ -108,3 +108,22 @@ def test_budget_admits_one_geometry_at_a_time():
         assert b.admit >= a.finish          # one admitted at a time
     for a, b in zip(free["records"], recs):
         _same(a.result, b.result)
+
+
+def test_native_server_matches_python_server():
+    """The C++ serving loop (madi_serve_*) gives the same sums as the Python loop
+    and as one launch per request."""
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300 import workloads as WL
+    from custom_madi_gb300.serving import NativeSimServer
+    cfg, cols, lay, e1, e2 = _setup()
+    lib, _ = WL.match_library(n_lib=2000)
+    reqs = [replace(r, arrival=0.0) for r in _requests(cfg, e1, e2, lib) if hasattr(r, "ensemble")]
+    py = _server(cfg, lay, lib).run(reqs, realtime=False)
+    nat = NativeSimServer(cfg, lay, cfg.direction_array(), boundary=N.MADI_BOUNDARY_PERIODIC,
+                          chunk_walkers=2048, launch_walkers=4096, n_slots=8)
+    out = nat.run(reqs, realtime=True)
+    nat.close()
+    for a, b in zip(py["records"], out["records"]):
+        _same(a.result, b.result)
+    assert out["walker_steps"] == sum(r.n_walkers for r in reqs) * cfg.n_steps

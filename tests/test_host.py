@@ -33,7 +33,8 @@ def test_struct_layout_matches_header(tmp_path):
     """ctypes mirrors == the C compiler's layout of the header structs."""
     structs = {"madi_geometry": N.MadiGeometry, "madi_walk_job": N.MadiWalkJob,
                "madi_walk_desc": N.MadiWalkDesc, "madi_match_desc": N.MadiMatchDesc,
-               "madi_launch_shape": N.MadiLaunchShape}
+               "madi_launch_shape": N.MadiLaunchShape, "madi_serve_config": N.MadiServeConfig,
+               "madi_serve_request": N.MadiServeRequest, "madi_serve_done": N.MadiServeDone}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/madi_gb300.h"', "int main(void){"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
