@@ -757,14 +757,48 @@ MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int
 
 // fp32 rescore of this thread's k candidates (staged in its buffer, as scan
 // positions) against the fp32 data; lowest caller index on ties.  Rows come
-// from the padded scan-order copy (at most eight aligned 16-byte loads each),
-// two candidates per step with all their loads in flight.
+// from the padded scan-order copy (RQ aligned 16-byte loads each, RQ >= F/4),
+// NC candidates per step with all their loads in flight.
+template <int K, bool FREE, int RQ, int NC>
+MADI_DEV void rescore_rows(const Plan& P, int64_t row, const float2* mybuf, int nv, float& best, int& bj,
+                           float& bs0) {
+    const int F = P.F, nq = (F + 3) / 4;
+    float m[4 * RQ];
+#pragma unroll
+    for (int k = 0; k < 4 * RQ; ++k) m[k] = k < F ? P.meas[row * F + k] : 0.f;
+#pragma unroll 1
+    for (int i = 0; i < nv; i += NC) {
+        int e[NC], j[NC];
+        float4 lv[NC][RQ];
+#pragma unroll
+        for (int u = 0; u < NC; ++u) {
+            const float2 c = (i + u < nv) ? mybuf[(i + u) * EPI_THREADS] : make_float2(__int_as_float(-1), 0.f);
+            e[u] = __float_as_int(c.x);
+            j[u] = __float_as_int(c.y);
+            const float4* L = reinterpret_cast<const float4*>(P.lrows + (size_t)(e[u] < 0 ? 0 : e[u]) * KPAD);
+#pragma unroll
+            for (int q = 0; q < RQ; ++q)
+                lv[u][q] = (e[u] >= 0 && q < nq) ? __ldg(L + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < NC; ++u) {
+            if (e[u] < 0) continue;
+            const float* lf = reinterpret_cast<const float*>(lv[u]);
+            float dot = 0.f, rr = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4 * RQ; ++k) { dot = fmaf(m[k], lf[k], dot); rr = fmaf(lf[k], lf[k], rr); }
+            const float s0 = FREE ? dot / fmaxf(rr, 1e-30f) : 1.f;
+            float res = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4 * RQ; ++k) { const float r = m[k] - s0 * lf[k]; res = fmaf(r, r, res); }
+            if (FREE && !(dot > 0.f)) res = 3.0e38f;
+            if (res < best || (res == best && j[u] < bj)) { best = res; bj = j[u]; bs0 = s0; }
+        }
+    }
+}
+
 template <int K, bool FREE>
 MADI_DEV void rescore(const Plan& P, int64_t row, const float2* mybuf, int nv, float& best, int& bj, float& bs0) {
-    const int F = P.F, nq = (F + 3) / 4;
-    float m[KPAD];
-#pragma unroll
-    for (int k = 0; k < KPAD; ++k) m[k] = k < F ? P.meas[row * F + k] : 0.f;
     // all K permutation lookups in flight at once; (scan position, caller index)
     // go back into the thread's buffer slots
     float2* wbuf = const_cast<float2*>(mybuf);
@@ -776,35 +810,8 @@ MADI_DEV void rescore(const Plan& P, int64_t row, const float2* mybuf, int nv, f
         const int j = valid ? __ldg(P.lperm + e) : -1;
         wbuf[i * EPI_THREADS] = make_float2(__int_as_float(valid ? e : -1), __int_as_float(j));
     }
-#pragma unroll 1
-    for (int i = 0; i < nv; i += 2) {
-        int e[2], j[2];
-        float4 lv[2][KPAD / 4];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const float2 c = mybuf[(i + u) * EPI_THREADS];
-            e[u] = __float_as_int(c.x);
-            j[u] = __float_as_int(c.y);
-            const float4* L = reinterpret_cast<const float4*>(P.lrows + (size_t)(e[u] < 0 ? 0 : e[u]) * KPAD);
-#pragma unroll
-            for (int q = 0; q < KPAD / 4; ++q)
-                lv[u][q] = (e[u] >= 0 && q < nq) ? __ldg(L + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            if (e[u] < 0) continue;
-            const float* lf = reinterpret_cast<const float*>(lv[u]);
-            float dot = 0.f, rr = 0.f;
-#pragma unroll
-            for (int k = 0; k < KPAD; ++k) { dot = fmaf(m[k], lf[k], dot); rr = fmaf(lf[k], lf[k], rr); }
-            const float s0 = FREE ? dot / fmaxf(rr, 1e-30f) : 1.f;
-            float res = 0.f;
-#pragma unroll
-            for (int k = 0; k < KPAD; ++k) { const float r = m[k] - s0 * lf[k]; res = fmaf(r, r, res); }
-            if (FREE && !(dot > 0.f)) res = 3.0e38f;
-            if (res < best || (res == best && j[u] < bj)) { best = res; bj = j[u]; bs0 = s0; }
-        }
-    }
+    if (P.F <= 24) rescore_rows<K, FREE, 6, 4>(P, row, mybuf, nv, best, bj, bs0);
+    else rescore_rows<K, FREE, KPAD / 4, 2>(P, row, mybuf, nv, best, bj, bs0);
 }
 
 template <int K, int MODE>
@@ -882,17 +889,17 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                 const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(acc * MMA_N + wg * TILE_N);
 #pragma unroll 1
                 for (int c = 0; c < TILE_N; c += WG_COLS) {
-                const uint32_t taddr = tbase + (uint32_t)c;
-                const float* ax = S.aux[acc][wg] + c;
-                const int jb = lt * TILE_N + c;
+                    const uint32_t taddr = tbase + (uint32_t)c;
+                    const float* ax = S.aux[acc][wg] + c;
+                    const int jb = lt * TILE_N + c;
                     float key[WG_COLS];
                     tmem_ld64(taddr, key);
                     if (MODE != MODE_FOLD) {
-    #pragma unroll
+#pragma unroll
                         for (int i = 0; i < WG_COLS; i += 4) {
                             const float4 q = *reinterpret_cast<const float4*>(ax + i);
                             const float qq[4] = {q.x, q.y, q.z, q.w};
-    #pragma unroll
+#pragma unroll
                             for (int u = 0; u < 4; ++u) {
                                 const float v = key[i + u];
                                 key[i + u] = FREE ? (-v * fabsf(v)) * qq[u] : fmaf(-2.f, v, qq[u]);
@@ -928,14 +935,14 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                     // fast path: no lane of the warp holds a candidate in this tile
                     {
                         float ext[8];   // eight independent running extremes, then a tree
-    #pragma unroll
+#pragma unroll
                         for (int i = 0; i < 8; ++i) ext[i] = key[i];
-    #pragma unroll
+#pragma unroll
                         for (int i = 8; i < WG_COLS; ++i)
                             ext[i & 7] = MODE == MODE_FOLD ? fmaxf(ext[i & 7], key[i]) : fminf(ext[i & 7], key[i]);
-    #pragma unroll
+#pragma unroll
                         for (int w = 4; w > 0; w >>= 1)
-    #pragma unroll
+#pragma unroll
                             for (int i = 0; i < w; ++i)
                                 ext[i] = MODE == MODE_FOLD ? fmaxf(ext[i], ext[i + w]) : fminf(ext[i], ext[i + w]);
                         const bool maybe = MODE == MODE_FOLD ? ext[0] > tthr_e : ext[0] < thr_e;
@@ -943,7 +950,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                     }
                     // eight independent 8-bit masks, then two 32-bit masks
                     uint32_t mk[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-    #pragma unroll
+#pragma unroll
                     for (int i = 0; i < WG_COLS; ++i) {
                         const bool hit = MODE == MODE_FOLD ? key[i] > tthr_e : key[i] < thr_e;
                         if (hit) mk[i >> 3] |= 1u << (i & 7);
@@ -952,7 +959,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                     uint32_t m1 = mk[4] | (mk[5] << 8) | (mk[6] << 16) | (mk[7] << 24);
                     const int nh0 = __popc(m0), nh1 = __popc(m1);
                     if (m0 | m1) {   // stage the keys for the append passes (lanes with hits only)
-    #pragma unroll
+#pragma unroll
                         for (int i = 0; i < WG_COLS; i += 4)
                             mystage[(i >> 2) * EPI_THREADS] = make_float4(key[i], key[i + 1], key[i + 2], key[i + 3]);
                     }
