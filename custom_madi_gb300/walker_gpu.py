@@ -505,6 +505,28 @@ def _pp_for(ens: Ensemble, kio: float, cfg: SimConfig) -> float:
     return _checked_pp(kio_to_pp(kio, ens.mean_AV, cfg))
 
 
+class WalkGraph:
+    """A batch's whole launch (work-counter and accumulator zeroing + the
+    persistent walk) captured once in a CUDA graph; ``replay()`` re-runs it on
+    the same device buffers with one host call."""
+
+    def __init__(self, batch: WalkBatch):
+        self.batch = batch
+        dev = batch.dev
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):                # warm-up outside the capture
+            batch.launch(side)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            batch.launch()
+
+    def replay(self) -> None:
+        self.graph.replay()
+
+
 def simulate_jobs(jobs: Sequence[WalkJob], cfg: SimConfig, columns: Tuple, *, dirs=None,
                   launch: Optional[LaunchConfig] = None, check: bool = True) -> list:
     """Walk every job in one persistent launch; per job cos / sin sums [n_cols, n_dirs]."""

@@ -204,3 +204,25 @@ def test_per_step_labels_match_oracle_on_fixed_stream(golden):
         m[s1] = np.inf
         assert np.min(np.abs(m - ann[s1])) < 1e-4, (w, j, float(np.min(np.abs(m - ann[s1]))))
     assert 0.2 < float(np.mean(tel["inside_trace"])) < 0.95
+
+
+def test_cuda_graph_replay_matches_eager_launch():
+    """The captured batched launch gives the same sums as an eager launch, every replay."""
+    import torch
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.walker_gpu import WalkBatch, WalkGraph, WalkJob, pair_layout
+    cfg, ens = _periodic_c0(3000)
+    _, ens2 = _periodic_c0(3000, seed=9, n_cells=40)
+    cols = S.build_columns(cfg)
+    lay = pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    jobs = [WalkJob(ens, 0.01, 42, 3000), WalkJob(ens2, 0.02, 7, 1000)]
+    b = WalkBatch(jobs, cfg, layout=lay, dirs=cfg.direction_array())
+    b.launch()
+    eager = [r["cos_fixed"].copy() for r in b.results()]
+    g = WalkGraph(b)
+    for _ in range(2):
+        g.replay()
+        torch.cuda.synchronize()
+        got = [r["cos_fixed"] for r in b.results()]
+        for a, c in zip(eager, got):
+            assert np.array_equal(a, c)
