@@ -43,7 +43,7 @@ MADI_CNT_N = len(CNT_NAMES)
 EXPORTED = (
     "madi_abi_version", "madi_last_error_string", "madi_classify", "madi_walk",
     "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_scratch_bytes",
-    "madi_kdtree_build", "madi_grid_build", "madi_walk_blocks_per_sm", "madi_walk_noalloc",
+    "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_walk_blocks_per_sm", "madi_walk_noalloc",
     "madi_walk_batched", "madi_autotune_load", "madi_autotune_store",
     "madi_serve_arena_bytes", "madi_serve_create", "madi_serve_submit", "madi_serve_poll",
     "madi_serve_release", "madi_serve_destroy",
@@ -66,6 +66,9 @@ class MadiGeometry(C.Structure):
         ("boundary", C.c_int32), ("has_cells", C.c_int32), ("pad0", C.c_int32),
         ("L", C.c_double), ("grid_h", C.c_double), ("safe_cap", C.c_double),
         ("source_lo", C.c_double), ("source_hi", C.c_double), ("coord_err", C.c_double),
+        ("off_cell_center", C.c_uint32), ("off_facet_begin", C.c_uint32),
+        ("off_facet_plane", C.c_uint32), ("off_facet_nbr", C.c_uint32),
+        ("n_cells", C.c_int32), ("pad1", C.c_int32), ("facet_tol", C.c_double),
     ]
 
 
@@ -164,8 +167,10 @@ def _declare(lib):
     lib.madi_kdtree_build.argtypes = [P, C.c_int32, P, P, P, P, P]
     lib.madi_grid_build.argtypes = [P, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
                                     P, P, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
+    lib.madi_facets_build.argtypes = [P, C.c_int32, C.c_int32, C.c_double, P, P, P, C.c_int64,
+                                      C.POINTER(C.c_int64), P]
     for name in ("madi_classify", "madi_walk", "madi_walk_noalloc", "madi_walk_batched", "madi_reduce_Y",
-                 "madi_match", "madi_kdtree_build", "madi_grid_build", "madi_autotune_load",
+                 "madi_match", "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_autotune_load",
                  "madi_autotune_store", "madi_serve_create", "madi_serve_submit", "madi_serve_poll",
                  "madi_serve_release", "madi_serve_destroy"):
         getattr(lib, name).restype = C.c_int

@@ -235,6 +235,231 @@ extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G
 }
 
 // ---------------------------------------------------------------------------
+// Cell facet tables.  A cell's Voronoi polytope is cut out of a cube of
+// half-side r around its seed by the bisector half-spaces {x : n.x <= h}
+// (x = q - c, u = c_j - c, n = u/|u|, h = |u|/2), taken in order of |u|.  The
+// polytope is kept in fp64 as faces with ordered vertex polygons.  A plane is
+// skipped only when every vertex lies below it by more than eps, so it is
+// redundant for the exact polytope too; the pass ends once |u|/2 exceeds the
+// largest vertex distance by eps, after which no plane can reach the cell.  The
+// candidate radius r doubles until it covers twice that distance.
+// ---------------------------------------------------------------------------
+namespace {
+struct P3 {
+    double x, y, z;
+};
+inline P3 operator+(P3 a, P3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline P3 operator-(P3 a, P3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline P3 operator*(double t, P3 a) { return {t * a.x, t * a.y, t * a.z}; }
+inline double dot(P3 a, P3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline P3 cross(P3 a, P3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double norm(P3 a) { return std::sqrt(dot(a, a)); }
+
+struct Face {
+    P3 n;
+    double h;
+    int32_t nbr;             // base cell across the plane; -2 for the bounding cube
+    std::vector<P3> poly;    // ordered vertices; empty when the plane only touches
+};
+
+struct Polytope {
+    std::vector<Face> faces;
+    double eps = 0.0;
+
+    void cube(double B) {
+        faces.clear();
+        const P3 ax[3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        for (int a = 0; a < 3; ++a)
+            for (int sgn = -1; sgn <= 1; sgn += 2) {
+                Face f;
+                f.n = (double)sgn * ax[a];
+                f.h = B;
+                f.nbr = -2;
+                const P3 u = ax[(a + 1) % 3], v = ax[(a + 2) % 3];
+                const P3 c = (sgn * B) * ax[a];
+                f.poly = {c + B * u + B * v, c - B * u + B * v, c - B * u - B * v, c + B * u - B * v};
+                faces.push_back(f);
+            }
+    }
+    double excess(P3 n, double h) const {
+        double m = -1e300;
+        for (const Face& f : faces)
+            for (const P3& v : f.poly) m = std::max(m, dot(n, v) - h);
+        return m;
+    }
+    double radius() const {
+        double r = 0.0;
+        for (const Face& f : faces)
+            for (const P3& v : f.poly) r = std::max(r, dot(v, v));
+        return std::sqrt(r);
+    }
+    // Vertices on the new plane, deduplicated and ordered by angle about n.
+    std::vector<P3> ring(std::vector<P3>& pts, P3 n) const {
+        std::vector<P3> u;
+        for (const P3& p : pts) {
+            bool dup = false;
+            for (const P3& q : u) dup |= norm(p - q) <= 1e-3 * eps;
+            if (!dup) u.push_back(p);
+        }
+        if (u.size() < 3) return {};
+        P3 c{0, 0, 0};
+        for (const P3& p : u) c = c + p;
+        c = (1.0 / (double)u.size()) * c;
+        const P3 t = std::fabs(n.x) < 0.6 ? P3{1, 0, 0} : P3{0, 1, 0};
+        P3 e1 = cross(n, t);
+        e1 = (1.0 / norm(e1)) * e1;
+        const P3 e2 = cross(n, e1);
+        std::vector<std::pair<double, size_t>> ang(u.size());
+        for (size_t i = 0; i < u.size(); ++i) ang[i] = {std::atan2(dot(u[i] - c, e2), dot(u[i] - c, e1)), i};
+        std::sort(ang.begin(), ang.end());
+        std::vector<P3> out(u.size());
+        for (size_t i = 0; i < u.size(); ++i) out[i] = u[ang[i].second];
+        return out;
+    }
+    void clip(P3 n, double h, int32_t nbr) {
+        std::vector<P3> fresh;
+        std::vector<Face> kept;
+        kept.reserve(faces.size() + 1);
+        const double on = 1e-6 * eps;
+        for (Face& f : faces) {
+            if (f.poly.empty()) { kept.push_back(std::move(f)); continue; }
+            const size_t m = f.poly.size();
+            std::vector<P3> out;
+            double smin = 1e300;
+            for (size_t i = 0; i < m; ++i) {
+                const P3 a = f.poly[i], b = f.poly[(i + 1) % m];
+                const double sa = dot(n, a) - h, sb = dot(n, b) - h;
+                smin = std::min(smin, sa);
+                if (sa <= 0.0) {
+                    out.push_back(a);
+                    if (sa >= -on) fresh.push_back(a);
+                }
+                if ((sa <= 0.0) != (sb <= 0.0)) {
+                    const P3 p = a + (sa / (sa - sb)) * (b - a);
+                    out.push_back(p);
+                    fresh.push_back(p);
+                }
+            }
+            if (out.size() >= 3) {
+                f.poly.swap(out);
+                kept.push_back(std::move(f));
+            } else if (smin <= eps) {       // reduced to an edge or a point: keep the plane
+                f.poly.clear();
+                kept.push_back(std::move(f));
+            }                               // else wholly beyond the new plane
+        }
+        Face nf;
+        nf.n = n;
+        nf.h = h;
+        nf.nbr = nbr;
+        nf.poly = ring(fresh, n);
+        kept.push_back(std::move(nf));
+        faces.swap(kept);
+    }
+};
+}  // namespace
+
+extern "C" madi_status madi_facets_build(const double* seeds, int32_t n, int32_t periodic, double L,
+                                         uint32_t* begin, float* planes, int32_t* nbr, int64_t capacity,
+                                         int64_t* total, double* stats) {
+    host::clear_error();
+    if (!seeds || n < 2 || !begin || !total || (periodic && !(L > 0.0)))
+        return host::fail(MADI_ERR_INVALID, "facets_build: bad arguments");
+    // candidate points: the seeds, plus their 26 neighbouring images when periodic
+    std::vector<double> pts;
+    const int K = periodic ? 1 : 0;
+    for (int kz = -K; kz <= K; ++kz)
+        for (int ky = -K; ky <= K; ++ky)
+            for (int kx = -K; kx <= K; ++kx)
+                for (int32_t i = 0; i < n; ++i) {
+                    const double* s = seeds + 4 * (size_t)i;
+                    pts.insert(pts.end(), {s[0] + kx * L, s[1] + ky * L, s[2] + kz * L, (double)i});
+                }
+    const int32_t np = (int32_t)(pts.size() / 4);
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int32_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], seeds[4 * (size_t)i + a]);
+            hi[a] = std::max(hi[a], seeds[4 * (size_t)i + a]);
+        }
+    const double ext = periodic ? L : std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-30});
+    const double spacing = std::cbrt(ext * ext * ext / n);
+    const Bins B = make_bins(pts.data(), np, spacing);
+    // periodic: images within +-1 box cover every candidate up to r = L
+    const double r_max = periodic ? L : 4.0 * ext;
+    int64_t count = 0;
+    double h_max = 0.0, reach = 0.0;
+    std::vector<std::pair<double, int32_t>> cand;
+    std::vector<const Face*> fl;
+    for (int32_t c = 0; c < n; ++c) {
+        const P3 x0{seeds[4 * (size_t)c], seeds[4 * (size_t)c + 1], seeds[4 * (size_t)c + 2]};
+        Polytope P;
+        bool closed = false;
+        for (double r = std::min(3.0 * spacing, r_max);; r = std::min(2.0 * r, r_max)) {
+            cand.clear();
+            const double blo[3] = {x0.x - r, x0.y - r, x0.z - r}, bhi[3] = {x0.x + r, x0.y + r, x0.z + r};
+            for_bins_in_box(B, blo, bhi, [&](int32_t j) {
+                const P3 u = P3{pts[4 * (size_t)j], pts[4 * (size_t)j + 1], pts[4 * (size_t)j + 2]} - x0;
+                const double d = norm(u);
+                if (d <= r && !(d == 0.0 && (int32_t)pts[4 * (size_t)j + 3] == c)) cand.push_back({d, j});
+            });
+            std::sort(cand.begin(), cand.end());
+            P.eps = 1e-9 * r;
+            P.cube(r);
+            bool ended = false;
+            for (const auto& cj : cand) {
+                if (cj.first == 0.0)
+                    return host::fail(MADI_ERR_GEOMETRY, "facets_build: seeds %d and %d coincide", c,
+                                      (int)pts[4 * (size_t)cj.second + 3]);
+                if (0.5 * cj.first > P.radius() + P.eps) { ended = true; break; }
+                const size_t j = (size_t)cj.second;
+                const P3 u = P3{pts[4 * j], pts[4 * j + 1], pts[4 * j + 2]} - x0;
+                const P3 nv = (1.0 / cj.first) * u;
+                const double h = 0.5 * cj.first;
+                if (P.excess(nv, h) < -P.eps) continue;
+                P.clip(nv, h, (int32_t)pts[4 * j + 3]);
+            }
+            if (ended || 2.0 * (P.radius() + P.eps) <= r) { closed = true; break; }
+            if (r >= r_max) break;
+        }
+        fl.clear();
+        if (closed) {
+            for (const Face& f : P.faces)
+                if (f.nbr >= 0) fl.push_back(&f);
+            std::sort(fl.begin(), fl.end(), [](const Face* a, const Face* b) { return a->h < b->h; });
+            reach = std::max(reach, P.radius());
+            for (const Face* f : fl) h_max = std::max(h_max, f->h);
+        }
+        begin[c] = (uint32_t)count;
+        const int64_t nf = closed ? (int64_t)fl.size() : 0;
+        const int64_t padded = std::max<int64_t>(4, (nf + 3) & ~3ll);
+        if (planes && count + padded <= capacity) {
+            for (int64_t k = 0; k < padded; ++k) {
+                float* o = planes + 4 * (size_t)(count + k);
+                if (k < nf) {
+                    const Face* f = fl[k];
+                    o[0] = (float)f->n.x; o[1] = (float)f->n.y; o[2] = (float)f->n.z; o[3] = (float)f->h;
+                    if (nbr) nbr[count + k] = f->nbr;
+                } else {
+                    o[0] = o[1] = o[2] = 0.0f;
+                    o[3] = closed ? 3.0e38f : -3.0e38f;
+                    if (nbr) nbr[count + k] = -1;
+                }
+            }
+        }
+        count += padded;
+        if (count > 0xFFFFFFFFll) return host::fail(MADI_ERR_CAPACITY, "facets_build: more than 2^32 facets");
+    }
+    begin[n] = (uint32_t)count;
+    *total = count;
+    if (stats) { stats[0] = h_max; stats[1] = reach; }
+    if (planes && count > capacity)
+        return host::fail(MADI_ERR_CAPACITY, "facets_build: capacity %lld < %lld facets", (long long)capacity,
+                          (long long)count);
+    return MADI_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Autotuner cache: one "key\ttile\tbps\tminb\tstage\trate" line per key.
 // ---------------------------------------------------------------------------
 namespace {

@@ -62,6 +62,13 @@ struct Geo {
     float cap;
     float cerr;                 // |fp32 seed - exact seed| per axis
     int n_seeds;
+    // cell facet table (n_cells = 0: none)
+    const float4* ccen;         // [n_cells] base seed x, y, z, alpha
+    const uint32_t* fbeg;       // [n_cells + 1]
+    const float4* fpl;          // [n_facets] unit normal, offset
+    const int32_t* fnbr;        // [n_facets] cell across the facet
+    int n_cells;
+    float ftol;                 // fp32 error of a facet margin, without the |w| term
 };
 
 MADI_DEV Geo make_geo(const madi_geometry& g, const unsigned char* base) {
@@ -80,6 +87,12 @@ MADI_DEV Geo make_geo(const madi_geometry& g, const unsigned char* base) {
     v.cap = (float)g.safe_cap;
     v.cerr = (float)g.coord_err;
     v.n_seeds = g.n_seeds;
+    v.ccen = reinterpret_cast<const float4*>(base + g.off_cell_center);
+    v.fbeg = reinterpret_cast<const uint32_t*>(base + g.off_facet_begin);
+    v.fpl = reinterpret_cast<const float4*>(base + g.off_facet_plane);
+    v.fnbr = reinterpret_cast<const int32_t*>(base + g.off_facet_nbr);
+    v.n_cells = g.n_cells;
+    v.ftol = (float)g.facet_tol;
     return v;
 }
 
@@ -205,31 +218,16 @@ MADI_DEV int f2o(float f) { const int i = __float_as_int(f); return i >= 0 ? i :
 MADI_DEV float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
 MADI_DEV float warp_minf(float v) { return o2f(__reduce_min_sync(MADI_FULL, f2o(v))); }
 
-// Label cache proven at a classified point p (walker displacement frame):
-// j* = the seed with the smallest margin m_j* (the nearest shifted facet),
-// R   = min(cap, min_{j != 1, j*} (m_j(p) - alpha_1) - tol).
-// Every q with |q - p| < R is on c1's side of all other facets by more than
-// alpha_1 (margins are 1-Lipschitz), so its label follows from the one exact
-// plane m_j*(q) = off - n.q:  >= alpha_1 intracellular (cell of c1),
-// in (-alpha_j*, alpha_1) extracellular; anything else needs a new pass.
-// The thresholds include the fp32 error of the plane evaluation.
-struct SlabCache {
-    float nx, ny, nz, off;
-    float in_thr, gap_hi, gap_lo;
-    float R2;
-};
-
+// Warp-cooperative margins pass for seed bi over the candidate list [b, e):
+// the lanes split the candidates, then vote.  Same decisions and error bands
+// as margins_pass.
 MADI_DEV int coop_margins(const Geo& g, float px, float py, float pz, uint32_t b, uint32_t e, int bi, int lane,
-                          float ex, float ey, float ez, int& inside, SlabCache& sc) {
+                          int& inside) {
     const float4 h1 = g.seed[bi];
     const float a1 = h1.w;
     const float bx = px - h1.x, by = py - h1.y, bz = pz - h1.z;
     const float t0 = g.cerr + MADI_EPS21 * 3.0f * (fabsf(bx) + fabsf(by) + fabsf(bz));
     bool not_near = false, out_sure = false, amb = false, found = false, tie = false;
-    // per lane: the candidate with the smallest margin, and the smallest (m - alpha_1 - tol)
-    // over all of its candidates (r_all) and over the others (r_excl)
-    float m_best = 3.0e38f, r_best = 3.0e38f, r_excl = 3.0e38f;
-    int j_best = -1;
     for (uint32_t k = b + lane; k < e; k += 32) {
         const int id = cand_id(g, k);
         if (id == bi) { found = true; continue; }
@@ -246,47 +244,12 @@ MADI_DEV int coop_margins(const Geo& g, float px, float py, float pz, uint32_t b
         out_sure |= dm < -tol;
         amb |= fabsf(dm) <= tol;
         tie |= m <= tol;
-        const float r = dm - tol;
-        if (m < m_best) {
-            r_excl = fminf(r_excl, r_best);
-            m_best = m; r_best = r; j_best = id;
-        } else {
-            r_excl = fminf(r_excl, r);
-        }
     }
-    sc.R2 = 0.f;
     if (__any_sync(MADI_FULL, not_near) || !__any_sync(MADI_FULL, found)) return CLS_NOT_NEAREST;
     if (__any_sync(MADI_FULL, tie)) return CLS_FALLBACK;
     const bool outside = __any_sync(MADI_FULL, out_sure);
     if (!outside && __any_sync(MADI_FULL, amb)) return CLS_FALLBACK;
     inside = outside ? 0 : 1;
-    // j*: lane holding the smallest margin
-    const float mmin = warp_minf(m_best);
-    const unsigned who = __ballot_sync(MADI_FULL, m_best == mmin);
-    const int jl = __ffs(who) - 1;
-    const float rest = warp_minf(lane == jl ? r_excl : fminf(r_best, r_excl));
-    const int js = __shfl_sync(MADI_FULL, j_best, jl);
-    const float R = fminf(rest, g.cap);
-    if (R > 0.f && js >= 0) {
-        const float4 hj = g.seed[js];
-        const float ux = hj.x - h1.x, uy = hj.y - h1.y, uz = hj.z - h1.z;
-        const float rsj = rsqrtf(fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
-        const float nx = ux * rsj, ny = uy * rsj, nz = uz * rsj;
-        const float aj = hj.w;
-        // plane in the displacement frame: m(q) = |u|/2 - n.(q - c1), c1 at e + (c1 - p)
-        const float cx = ex - bx, cy = ey - by, cz = ez - bz;
-        const float hu = 0.5f / rsj;
-        sc.nx = nx; sc.ny = ny; sc.nz = nz;
-        sc.off = hu + fmaf(nx, cx, fmaf(ny, cy, nz * cz));
-        const float dist = fabsf(bx) + fabsf(by) + fabsf(bz) + R;
-        const float T = 2.0f * (g.cerr * (2.0f + 4.0f * dist * rsj)
-                                + MADI_EPS21 * (fabsf(ex) + fabsf(ey) + fabsf(ez) + fabsf(cx) + fabsf(cy) + fabsf(cz)
-                                                + 2.0f * dist + hu + a1 + aj));
-        sc.in_thr = a1 + T;
-        sc.gap_hi = a1 - T;
-        sc.gap_lo = -aj + T;
-        sc.R2 = R * R * (1.0f - MADI_EPS19);
-    }
     return CLS_OK;
 }
 
@@ -314,24 +277,90 @@ MADI_DEV int coop_nearest(const Geo& g, float px, float py, float pz, uint32_t b
     return CLS_OK;
 }
 
-// Classify point p (walker displacement e) cooperatively; guess = nearest seed
-// of an earlier nearby point or -1.  On CLS_OK sc holds the label cache.
-MADI_DEV int coop_classify(const Geo& g, float px, float py, float pz, float ex, float ey, float ez, int guess,
-                           int lane, int& seed1, int& inside, SlabCache& sc) {
-    sc.R2 = 0.f;
+// Classify point p cooperatively; guess = a seed likely to be nearest or -1.
+MADI_DEV int coop_classify(const Geo& g, float px, float py, float pz, int guess, int lane, int& seed1, int& inside) {
     const int v = voxel_of(g, px, py, pz);
     const uint32_t b = g.off[v], e = g.off[v + 1];
     if (b >= e) return CLS_ERROR;
     if (guess >= 0) {
-        const int st = coop_margins(g, px, py, pz, b, e, guess, lane, ex, ey, ez, inside, sc);
+        const int st = coop_margins(g, px, py, pz, b, e, guess, lane, inside);
         if (st != CLS_NOT_NEAREST) { seed1 = guess; return st; }
     }
     int bi = 0;
     const int st = coop_nearest(g, px, py, pz, b, e, lane, bi);
     if (st != CLS_OK) return st;
     seed1 = bi;
-    const int st2 = coop_margins(g, px, py, pz, b, e, bi, lane, ex, ey, ez, inside, sc);
+    const int st2 = coop_margins(g, px, py, pz, b, e, bi, lane, inside);
     return st2 == CLS_NOT_NEAREST ? CLS_FALLBACK : st2;
+}
+
+// ---------------------------------------------------------------------------
+// Facet-plane labels.  For q in the Voronoi cell of base seed c the margins
+// to all other seeds are bounded below by the distances to the cell's own
+// facet planes, m_k(q) = h_k - n_k.w with w = q - c (periodic: the nearest
+// image), so the cell's facet list alone decides the SI Eq. S2 label:
+//   min_k m_k > T and min_k m_k - alpha_c > T   -> intracellular, cell c
+//   min_k m_k > T and min_k m_k - alpha_c < -T  -> extracellular, Voronoi cell c
+//   min_k m_k < -T                              -> q is in another cell
+// T bounds the fp32 error of m_k (seed rounding, stored n and h, the
+// subtraction and wrap of w, three fused multiply-adds):
+//   |m - m_exact| <= 2 e + 2^-21 (h + |w|_1 + L),   e = per-axis seed error,
+// taken twice; ftol holds the part without |w|_1.
+// ---------------------------------------------------------------------------
+enum { FACET_OUT = 0, FACET_IN = 1, FACET_LEFT = -1, FACET_BAND = -2 };
+
+MADI_DEV float facet_m(const float4 f, float wx, float wy, float wz) {
+    return fmaf(-f.z, wz, fmaf(-f.y, wy, fmaf(-f.x, wx, f.w)));
+}
+
+// Label of q from the facets of cell c; on FACET_LEFT, nb = the cell across
+// the most violated facet (-1 when the cell has no closed polytope).
+template <bool PERIODIC>
+MADI_DEV int facet_label(const Geo& g, float qx, float qy, float qz, int c, int& nb) {
+    const float4 cc = g.ccen[c];
+    float wx = qx - cc.x, wy = qy - cc.y, wz = qz - cc.z;
+    if (PERIODIC) {
+        const float hl = 0.5f * g.L;
+        wx = wx > hl ? wx - g.L : (wx < -hl ? wx + g.L : wx);
+        wy = wy > hl ? wy - g.L : (wy < -hl ? wy + g.L : wy);
+        wz = wz > hl ? wz - g.L : (wz < -hl ? wz + g.L : wz);
+    }
+    const uint32_t b = g.fbeg[c], e = g.fbeg[c + 1];
+    float mmin = 3.0e38f;
+    for (uint32_t k = b; k < e; k += 4) {
+        const float4 f0 = g.fpl[k], f1 = g.fpl[k + 1], f2 = g.fpl[k + 2], f3 = g.fpl[k + 3];
+        const float m01 = fminf(facet_m(f0, wx, wy, wz), facet_m(f1, wx, wy, wz));
+        const float m23 = fminf(facet_m(f2, wx, wy, wz), facet_m(f3, wx, wy, wz));
+        mmin = fminf(mmin, fminf(m01, m23));
+    }
+    const float T = fmaf(2.0f * MADI_EPS21, fabsf(wx) + fabsf(wy) + fabsf(wz), g.ftol);
+    if (mmin > T) {
+        const float d = mmin - cc.w;
+        if (d > T) return FACET_IN;
+        if (d < -T) return FACET_OUT;
+        return FACET_BAND;
+    }
+    if (mmin >= -T) return FACET_BAND;
+    nb = -1;
+    for (uint32_t k = b; k < e; ++k)
+        if (facet_m(g.fpl[k], wx, wy, wz) == mmin) { nb = g.fnbr[k]; break; }
+    return FACET_LEFT;
+}
+
+// Label of q starting from cell c: up to three moves across violated facets.
+// Returns FACET_IN / FACET_OUT with cell_q set, or a negative code when the
+// voxel-grid classifier has to decide.
+template <bool PERIODIC>
+MADI_DEV int facet_walk(const Geo& g, float qx, float qy, float qz, int c, int& cell_q) {
+    int nb = -1;
+    int r = facet_label<PERIODIC>(g, qx, qy, qz, c, nb);
+#pragma unroll 1
+    for (int hop = 0; hop < 3 && r == FACET_LEFT && nb >= 0; ++hop) {
+        c = nb;
+        r = facet_label<PERIODIC>(g, qx, qy, qz, c, nb);
+    }
+    cell_q = c;
+    return r;
 }
 
 // ---------------------------------------------------------------------------

@@ -36,7 +36,6 @@ struct TileShared {
     long long* acc;       // [2 n_out] fixed-point cos / sin sums of the tile
     unsigned int* occ;    // [n_grid] inside counts
     const Snap* snap;     // [n_grid] moment coefficients
-    SlabCache* pend;      // [blockDim.x] label cache of this step's refresh, per walker
     double* auxd;         // [3][blockDim.x] Y' at the last storage point (fp64)
     float* auxf;          // [3 + 3 NP][blockDim.x] interval-start displacement, moments dM
     uint32_t* auxc;       // [3][blockDim.x] rare counters: fp64 fallbacks, accepted, rejected crossings
@@ -86,11 +85,8 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
     const float x0f = px, y0f = py, z0f = pz;
     // ---- state ----
     float dx = 0.f, dy = 0.f, dz = 0.f;           // unwrapped displacement from x0
-    float rx = 0.f, ry = 0.f, rz = 0.f;           // label-cache centre (displacement frame)
-    SlabCache sc;
-    sc.R2 = 0.f; sc.nx = sc.ny = sc.nz = sc.off = sc.in_thr = sc.gap_hi = sc.gap_lo = 0.f;
-    int cell = 0, inside = 0, seed = -1;          // seed: nearest seed at the last classification
-    int cache_cell = 0;
+    int cell = 0, inside = 0;                     // Voronoi cell of the position and its label
+    const bool facets = cells && g.n_cells > 0;
     bool dead = !active;
     bool frozen = !active;
     uint32_t n_full = 0, n_t1 = 0, escaped = 0, cerr = 0;
@@ -106,19 +102,17 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
             const float sy = __shfl_sync(MADI_FULL, py, src);
             const float sz = __shfl_sync(MADI_FULL, pz, src);
             int s1 = 0, in = 0;
-            SlabCache c;
-            const int st = coop_classify(g, sx, sy, sz, 0.f, 0.f, 0.f, -1, lane, s1, in, c);
-            if (lane == src) { my_st = st; my_s1 = s1; my_in = in; ts.pend[threadIdx.x] = c; }
+            const int st = coop_classify(g, sx, sy, sz, -1, lane, s1, in);
+            if (lane == src) { my_st = st; my_s1 = s1; my_in = in; }
         }
         __syncwarp();
         if (active) {
             if (my_st == CLS_FALLBACK) {
                 my_st = classify_list_f64(g, px, py, pz, my_s1, my_in);
-                ts.pend[threadIdx.x].R2 = 0.f;
                 ++AUX_C(0);
             }
             if (my_st != CLS_OK) { cerr = 1; dead = true; }
-            else { cell = cell_of(g, my_s1); inside = my_in; sc = ts.pend[threadIdx.x]; seed = my_s1; cache_cell = cell; }
+            else { cell = cell_of(g, my_s1); inside = my_in; }
             ++n_full;
         }
     }
@@ -188,16 +182,12 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
             }
         }
         const float ex = dx + nx, ey = dy + ny, ez = dz + nz;
-        // ---- label cache: inside the proven sphere, one plane decides ----
+        // ---- label from the facet planes of the current cell (and its neighbours) ----
         bool t1 = false;
-        int t1_in = 0;
-        if (ok && cells) {
-            const float tx = ex - rx, ty = ey - ry, tz = ez - rz;
-            if (fmaf(tx, tx, fmaf(ty, ty, tz * tz)) < sc.R2) {
-                const float m = sc.off - fmaf(sc.nx, ex, fmaf(sc.ny, ey, sc.nz * ez));
-                if (m >= sc.in_thr) { t1 = true; t1_in = 1; }
-                else if (m < sc.gap_hi && m > sc.gap_lo) { t1 = true; t1_in = 0; }
-            }
+        int t1_in = 0, t1_cell = cell;
+        if (ok && facets) {
+            const int r = facet_walk<PERIODIC>(g, qx, qy, qz, cell, t1_cell);
+            if (r >= 0) { t1 = true; t1_in = r; }
         }
         // ---- full classifications of this step, one warp-cooperative pass each ----
         const bool need = ok && cells && !t1;
@@ -207,30 +197,24 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
             const float sx = __shfl_sync(MADI_FULL, qx, src);
             const float sy = __shfl_sync(MADI_FULL, qy, src);
             const float sz = __shfl_sync(MADI_FULL, qz, src);
-            const float tx = __shfl_sync(MADI_FULL, ex, src);
-            const float ty = __shfl_sync(MADI_FULL, ey, src);
-            const float tz = __shfl_sync(MADI_FULL, ez, src);
-            const int sg = __shfl_sync(MADI_FULL, seed, src);
+            const int sg = __shfl_sync(MADI_FULL, cell, src);
             int s1 = 0, in = 0;
-            SlabCache c;
-            const int st = coop_classify(g, sx, sy, sz, tx, ty, tz, sg, lane, s1, in, c);
-            if (lane == src) { my_st = st; my_s1 = s1; my_in = in; ts.pend[threadIdx.x] = c; }
+            const int st = coop_classify(g, sx, sy, sz, sg, lane, s1, in);
+            if (lane == src) { my_st = st; my_s1 = s1; my_in = in; }
         }
         __syncwarp();
         if (ok) {
             int ncell = 0, nin = 0;
-            bool refreshed = false;
             if (t1) {
-                ncell = cache_cell; nin = t1_in; ++n_t1;
+                ncell = t1_cell; nin = t1_in; ++n_t1;
             } else if (need) {
                 if (my_st == CLS_FALLBACK) {
                     my_st = classify_list_f64(g, qx, qy, qz, my_s1, my_in);
-                    ts.pend[threadIdx.x].R2 = 0.f;
                     ++AUX_C(0);
                 }
                 ++n_full;
                 if (my_st != CLS_OK) { cerr = 1; dead = true; }
-                else { ncell = cell_of(g, my_s1); nin = my_in; refreshed = true; }
+                else { ncell = cell_of(g, my_s1); nin = my_in; }
             }
             if (!dead) {
                 int m = 0;
@@ -256,7 +240,6 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
                     px = qx; py = qy; pz = qz;
                     dx = ex; dy = ey; dz = ez;
                     cell = ncell; inside = nin;
-                    if (refreshed) { rx = ex; ry = ey; rz = ez; sc = ts.pend[threadIdx.x]; seed = my_s1; cache_cell = ncell; }
                 }
             }
         }
@@ -380,8 +363,7 @@ __global__ void __launch_bounds__(256, MINB) walk_f32_kernel(const madi_walk_des
     ts.snap = snap;
     unsigned char* aux = smem + d.stage_smem + 16 * n_out + 12 * ((d.n_grid + 3) & ~3);
     ts.auxd = reinterpret_cast<double*>(aux);
-    ts.pend = reinterpret_cast<SlabCache*>(aux + 24 * nthr);
-    ts.auxf = reinterpret_cast<float*>(aux + 24 * nthr + (int)sizeof(SlabCache) * nthr);
+    ts.auxf = reinterpret_cast<float*>(aux + 24 * nthr);
     ts.auxc = reinterpret_cast<uint32_t*>(ts.auxf + (3 + 3 * NP) * nthr);
 
     for (int j = tid; j < d.n_grid; j += nthr) {
@@ -592,7 +574,7 @@ extern "C" int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walker
 static int64_t fused_smem(const madi_walk_desc* d, int np) {
     const int64_t n_out = (int64_t)d->n_pairs * d->n_b * d->n_dirs;
     return (int64_t)d->stage_smem + 16ll * n_out + 12ll * ((d->n_grid + 3) & ~3) +
-           ((int64_t)sizeof(SlabCache) + 24 + 4 * (3 + 3 * np) + 12) * d->tile_walkers;
+           (24 + 4 * (3 + 3 * np) + 12) * d->tile_walkers;
 }
 
 template <int OUT, bool PER, int NP, int MINB>

@@ -252,6 +252,29 @@ def build_voxel_grid(seeds_xyza: np.ndarray, G: int, h: float, eps: float, cap: 
     return offsets, ids[: int(total.value)], bool(u32)
 
 
+def build_facets(seeds_xyza: np.ndarray, periodic: bool, L: float):
+    """Voronoi facet table of every base cell (madi_facets_build):
+    (begin uint32 [n+1], planes float32 [T, 4], nbr int32 [T], h_max, reach)."""
+    s = np.ascontiguousarray(seeds_xyza, dtype=np.float64)
+    n = len(s)
+    begin = np.zeros(n + 1, dtype=np.uint32)
+    cap = 48 * n
+    for _ in range(2):
+        planes = np.zeros((cap, 4), dtype=np.float32)
+        nbr = np.zeros(cap, dtype=np.int32)
+        total = C.c_int64(0)
+        stats = np.zeros(2, dtype=np.float64)
+        st = N.lib().madi_facets_build(s.ctypes.data, n, 1 if periodic else 0, float(L), begin.ctypes.data,
+                                       planes.ctypes.data, nbr.ctypes.data, cap, C.byref(total), stats.ctypes.data)
+        if st == N.MADI_ERR_CAPACITY and total.value > cap:
+            cap = int(total.value)
+            continue
+        N.check(st, "madi_facets_build")
+        t = int(total.value)
+        return begin, planes[:t], nbr[:t], float(stats[0]), float(stats[1])
+    raise RuntimeError("madi_facets_build: facet count changed between calls")
+
+
 # ---------------------------------------------------------------------------
 # Ensemble
 # ---------------------------------------------------------------------------
@@ -374,14 +397,31 @@ class DeviceGeometry:
             offsets, ids, u32 = build_voxel_grid(xyza, G, h, eps, float(ens.safe_cap))
         self.grid_total = int(len(ids))
         self.candidates_mean = float(len(ids)) / float(G ** 3)
+        # facet table of the base cells (periodic: the first n_cells seeds, images generated natively)
+        periodic = ens.boundary_mode == "periodic"
+        if ens.is_free_water:
+            n_cells, centers, fbeg = 0, np.zeros((0, 4), np.float32), np.zeros(1, np.uint32)
+            fpl, fnbr, h_max = np.zeros((0, 4), np.float32), np.zeros(0, np.int32), 0.0
+        else:
+            n_cells = int(cellid.max()) + 1
+            base = xyza[:n_cells]
+            if not np.array_equal(cellid[:n_cells], np.arange(n_cells)):
+                raise RuntimeError("classifier seeds must list the base cells first")
+            fbeg, fpl, fnbr, h_max, self.facet_reach = build_facets(base, periodic, float(ens.L))
+            centers = base.astype(np.float32)
+        self.n_cells = n_cells
+        self.facets_mean = float(np.count_nonzero(fnbr >= 0)) / max(n_cells, 1)
+        # |m - m_exact| <= 2 e + 2^-21 (h + |w|_1 + L) for fp32 facet margins, taken twice
+        a_max = float(np.max(ann)) if n else 0.0
+        self.facet_tol = 2.0 * (2.0 * self.coord_err + 2.0 ** -21 * (h_max + a_max + float(ens.L)))
 
         def pad16(b: bytes) -> bytes:
             return b + b"\0" * ((-len(b)) % 16)
 
-        parts = [hi.tobytes(), pad16(cellid.tobytes()), pad16(offsets.tobytes()), pad16(ids.tobytes())]
-        off_cell = len(parts[0])
-        off_go = off_cell + len(parts[1])
-        off_gi = off_go + len(parts[2])
+        parts = [hi.tobytes(), pad16(cellid.tobytes()), pad16(offsets.tobytes()), pad16(ids.tobytes()),
+                 pad16(centers.tobytes()), pad16(fbeg.tobytes()), pad16(fpl.tobytes()), pad16(fnbr.tobytes())]
+        offs = np.cumsum([0] + [len(p) for p in parts])
+        off_cell, off_go, off_gi = int(offs[1]), int(offs[2]), int(offs[3])
         blob = b"".join(parts)
         self.stage = torch.frombuffer(bytearray(blob), dtype=torch.uint8).to(device)
         self.seed_f64 = torch.from_numpy(xyza).to(device)
@@ -406,6 +446,9 @@ class DeviceGeometry:
         s.source_lo = float(ens.source_lo)
         s.source_hi = float(ens.source_hi)
         s.coord_err = self.coord_err
+        s.off_cell_center, s.off_facet_begin, s.off_facet_plane, s.off_facet_nbr = (int(o) for o in offs[4:8])
+        s.n_cells = n_cells
+        s.facet_tol = self.facet_tol
         self.struct = s
         self.stage_bytes = len(blob)
 

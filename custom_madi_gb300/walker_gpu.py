@@ -360,7 +360,7 @@ class WalkBatch:
         # shared-memory staging (every geometry that fits the per-CTA budget) and persistent grid
         budget = lc.stage_budget if lc.staged is not False else 0
         np_ = 8 if (layout is not None and layout.n_pairs > 4) else 4
-        fused_extra = 16 * self.n_out + 12 * ((cfg.n_grid + 3) // 4 * 4) + (32 + 24 + 4 * (3 + 3 * np_) + 12) * tw
+        fused_extra = 16 * self.n_out + 12 * ((cfg.n_grid + 3) // 4 * 4) + (24 + 4 * (3 + 3 * np_) + 12) * tw
         fits = [g.stage_bytes for g in geoms if g.stage_bytes + fused_extra <= min(budget, 227 * 1024)]
         d.stage_smem = ((max(fits) + 15) // 16 * 16) if (fits and precision == 32) else 0
         self.smem_bytes = d.stage_smem + fused_extra

@@ -87,6 +87,15 @@ typedef struct madi_geometry {
     double   source_lo;            /* walkers start uniform in [lo, hi)^3         */
     double   source_hi;
     double   coord_err;            /* bound on |fp32 seed - fp64 seed| per axis   */
+    /* Cell facet table (madi_facets_build), byte offsets inside stage.  With
+     * n_cells = 0 the walker labels every step with the voxel-grid classifier. */
+    uint32_t off_cell_center;      /* float4 [n_cells]: base seed x, y, z, alpha  */
+    uint32_t off_facet_begin;      /* uint32 [n_cells + 1]: facet range per cell  */
+    uint32_t off_facet_plane;      /* float4 [n_facets]: unit normal n, offset h  */
+    uint32_t off_facet_nbr;        /* int32 [n_facets]: cell across the facet     */
+    int32_t  n_cells;              /* cells in the table (0 = no table)           */
+    int32_t  pad1;
+    double   facet_tol;            /* fp32 error of h - n.w, without the |w| term */
 } madi_geometry;
 
 /* Replaces Ensemble.classify_cpu (madi/ensemble.py:213-256) and the device
@@ -286,6 +295,27 @@ madi_status madi_kdtree_build(const double* seeds_xyz, int32_t n, int32_t* node_
 madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h,
                             double eps, double safe_cap, uint32_t* offsets,
                             void* ids, int32_t ids_u32, int64_t capacity, int64_t* total);
+
+/* Facet table of every cell's Voronoi polytope.  The reference has no
+ * counterpart: its classifier searches a KD tree at every step, while the
+ * walker labels most steps from the planes of the cell it is in.
+ * seeds: [n][4] x, y, z, alpha of the base cells (periodic: in [0, L)^3, the
+ * images are generated here).  For cell c and facet k,
+ *   m_k(q) = h_k - n_k.(q - c)
+ * is the signed distance of q to the bisector plane between c and the cell
+ * nbr_k (periodic: q - c is the nearest image).  Every Voronoi facet of the
+ * cell is listed; planes that only touch the polytope may be listed too.  Each
+ * cell's range begin[c] .. begin[c + 1] is padded to a multiple of 4 with
+ * (0, 0, 0, 3e38) and nbr -1.  A cell whose polytope cannot be closed by the
+ * other seeds (an outer cell of a finite population) gets one padded group
+ * with h = -3e38, which sends every step there to the voxel-grid classifier.
+ * begin: [n + 1]; planes: [capacity][4] (fp32, n_k then h_k); nbr: [capacity].
+ * If capacity < *total the call fails with MADI_ERR_CAPACITY and *total holds
+ * the size needed.  stats (optional, [2]): the largest h over all facets and
+ * the largest distance from a seed to a vertex of its closed cell. */
+madi_status madi_facets_build(const double* seeds, int32_t n, int32_t periodic, double L,
+                              uint32_t* begin, float* planes, int32_t* nbr,
+                              int64_t capacity, int64_t* total, double* stats);
 
 /* ------------------------------------------------------------------------ */
 /* Serving loop (no counterpart in the reference)                           */
