@@ -66,7 +66,7 @@ class MadiGeometry(C.Structure):
         ("boundary", C.c_int32), ("has_cells", C.c_int32), ("pad0", C.c_int32),
         ("L", C.c_double), ("grid_h", C.c_double), ("safe_cap", C.c_double),
         ("source_lo", C.c_double), ("source_hi", C.c_double), ("coord_err", C.c_double),
-        ("off_cell_center", C.c_uint32), ("off_facet_begin", C.c_uint32),
+        ("off_cell_center", C.c_uint32), ("facet_stride", C.c_uint32),
         ("off_facet_plane", C.c_uint32), ("off_facet_nbr", C.c_uint32),
         ("n_cells", C.c_int32), ("pad1", C.c_int32), ("facet_tol", C.c_double),
     ]

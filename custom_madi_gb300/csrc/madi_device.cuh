@@ -64,9 +64,9 @@ struct Geo {
     int n_seeds;
     // cell facet table (n_cells = 0: none)
     const float4* ccen;         // [n_cells] base seed x, y, z, alpha
-    const uint32_t* fbeg;       // [n_cells + 1]
-    const float4* fpl;          // [n_facets] unit normal, offset
-    const int32_t* fnbr;        // [n_facets] cell across the facet
+    int fstride;                // facet slots per cell (multiple of 32)
+    const float4* fpl;          // [n_cells][fstride] unit normal, offset
+    const int32_t* fnbr;        // [n_cells][fstride] cell across the facet
     int n_cells;
     float ftol;                 // fp32 error of a facet margin, without the |w| term
 };
@@ -88,7 +88,7 @@ MADI_DEV Geo make_geo(const madi_geometry& g, const unsigned char* base) {
     v.cerr = (float)g.coord_err;
     v.n_seeds = g.n_seeds;
     v.ccen = reinterpret_cast<const float4*>(base + g.off_cell_center);
-    v.fbeg = reinterpret_cast<const uint32_t*>(base + g.off_facet_begin);
+    v.fstride = (int)g.facet_stride;
     v.fpl = reinterpret_cast<const float4*>(base + g.off_facet_plane);
     v.fnbr = reinterpret_cast<const int32_t*>(base + g.off_facet_nbr);
     v.n_cells = g.n_cells;
@@ -313,55 +313,15 @@ MADI_DEV float facet_m(const float4 f, float wx, float wy, float wz) {
     return fmaf(-f.z, wz, fmaf(-f.y, wy, fmaf(-f.x, wx, f.w)));
 }
 
-// Label of q from the facets of cell c; on FACET_LEFT, nb = the cell across
-// the most violated facet (-1 when the cell has no closed polytope).
-template <bool PERIODIC>
-MADI_DEV int facet_label(const Geo& g, float qx, float qy, float qz, int c, int& nb) {
-    const float4 cc = g.ccen[c];
-    float wx = qx - cc.x, wy = qy - cc.y, wz = qz - cc.z;
-    if (PERIODIC) {
-        const float hl = 0.5f * g.L;
-        wx = wx > hl ? wx - g.L : (wx < -hl ? wx + g.L : wx);
-        wy = wy > hl ? wy - g.L : (wy < -hl ? wy + g.L : wy);
-        wz = wz > hl ? wz - g.L : (wz < -hl ? wz + g.L : wz);
-    }
-    const uint32_t b = g.fbeg[c], e = g.fbeg[c + 1];
-    float mmin = 3.0e38f;
-    for (uint32_t k = b; k < e; k += 4) {
-        const float4 f0 = g.fpl[k], f1 = g.fpl[k + 1], f2 = g.fpl[k + 2], f3 = g.fpl[k + 3];
-        const float m01 = fminf(facet_m(f0, wx, wy, wz), facet_m(f1, wx, wy, wz));
-        const float m23 = fminf(facet_m(f2, wx, wy, wz), facet_m(f3, wx, wy, wz));
-        mmin = fminf(mmin, fminf(m01, m23));
-    }
-    const float T = fmaf(2.0f * MADI_EPS21, fabsf(wx) + fabsf(wy) + fabsf(wz), g.ftol);
-    if (mmin > T) {
-        const float d = mmin - cc.w;
-        if (d > T) return FACET_IN;
-        if (d < -T) return FACET_OUT;
-        return FACET_BAND;
-    }
-    if (mmin >= -T) return FACET_BAND;
-    nb = -1;
-    for (uint32_t k = b; k < e; ++k)
-        if (facet_m(g.fpl[k], wx, wy, wz) == mmin) { nb = g.fnbr[k]; break; }
-    return FACET_LEFT;
-}
-
-// Label of q starting from cell c: up to three moves across violated facets.
-// Returns FACET_IN / FACET_OUT with cell_q set, or a negative code when the
-// voxel-grid classifier has to decide.
-template <bool PERIODIC>
-MADI_DEV int facet_walk(const Geo& g, float qx, float qy, float qz, int c, int& cell_q) {
-    int nb = -1;
-    int r = facet_label<PERIODIC>(g, qx, qy, qz, c, nb);
-#pragma unroll 1
-    for (int hop = 0; hop < 3 && r == FACET_LEFT && nb >= 0; ++hop) {
-        c = nb;
-        r = facet_label<PERIODIC>(g, qx, qy, qz, c, nb);
-    }
-    cell_q = c;
-    return r;
-}
+// Four smallest margins of a full facet pass (facet slots k1..k3), the
+// point w relative to the cell centre cc, and the error bound T at w.
+struct FacetTop {
+    float m1, m2, m3, m4;
+    uint32_t k1, k2, k3;
+    int nb1;                    // cell across facet k1
+    float wx, wy, wz, T;
+    float4 cc;
+};
 
 // ---------------------------------------------------------------------------
 // fp64 rule on the voxel candidate list: nearest seed, then every seed within

@@ -38,6 +38,7 @@ struct TileShared {
     const Snap* snap;     // [n_grid] moment coefficients
     double* auxd;         // [3][blockDim.x] Y' at the last storage point (fp64)
     float* auxf;          // [3 + 3 NP][blockDim.x] interval-start displacement, moments dM
+    float4* fc;           // [5][blockDim.x] per-walker label cache (two facet planes + sphere)
     uint32_t* auxc;       // [3][blockDim.x] rare counters: fp64 fallbacks, accepted, rejected crossings
 };
 
@@ -47,6 +48,157 @@ struct TileShared {
 #define AUX_A(k) ts.auxf[(k) * blockDim.x + threadIdx.x]
 #define AUX_M(p, k) ts.auxf[(3 + 3 * (p) + (k)) * blockDim.x + threadIdx.x]
 #define AUX_C(k) ts.auxc[(k) * blockDim.x + threadIdx.x]
+#define FC(k) ts.fc[(k) * blockDim.x + threadIdx.x]
+
+// Per-walker label cache, built at a point q0 of cell c by a full facet pass
+// with margins m1 <= m2 <= m3 <= m4 (facets k1, k2, k3; error bound T0 at q0):
+//   FC(0..2) = facets k1, k2, k3 (n, h);   FC(3) = (w0, R^2);
+//   FC(4) = (c, alpha_c + Tm);   FC(5) = (alpha_c - Tm, Tm, c, cell across k1),
+// Tm = 3 T0.  Every other facet k has exact m_k(q0) >= m4 - T0 and is
+// 1-Lipschitz, so for |w - w0| < R = m4 - alpha_c - 8 T0 it stays above
+// alpha_c + T(q) (T(q) <= Tm there, and the w rounding of both points adds at
+// most T(q) + T0): for q in the Voronoi cell of c (all cached margins > Tm)
+// the label follows from the three cached margins alone, as in facet_label.
+// A point across a cached facet goes to a full pass (the facet list of c does
+// not bound the seeds beyond it), started in the cell across k1 when k1 is
+// the facet crossed.
+constexpr int FC_BYTES_PER_WALKER = 6 * 16;
+
+// Writes the cache of the walker in thread `w` (this CTA) from a full pass.
+MADI_DEV void fc_build(const TileShared& ts, int w, const FacetTop& t, int c, float L, const Geo& g) {
+    const float Tm = 3.0f * t.T;
+    const float R = fminf(t.m4 - t.cc.w - 8.0f * t.T, L);
+    float4* f = ts.fc + w;
+    const int n = blockDim.x;
+    f[0] = g.fpl[t.k1];
+    f[n] = g.fpl[t.k2];
+    f[2 * n] = g.fpl[t.k3];
+    f[3 * n] = make_float4(t.wx, t.wy, t.wz, R > 0.f ? R * R * (1.0f - MADI_EPS19) : 0.f);
+    f[4 * n] = make_float4(t.cc.x, t.cc.y, t.cc.z, t.cc.w + Tm);
+    f[5 * n] = make_float4(t.cc.w - Tm, Tm, __int_as_float(c), __int_as_float(t.nb1));
+}
+
+// (m1, k1) <= (m2, k2) <= (m3, k3) <= m4 after adding margin m of facet slot
+// k with neighbour nb (m < m4); nb1 follows k1.
+MADI_DEV void top4_insert(float m, uint32_t k, int nb, FacetTop& t) {
+    const bool lt1 = m < t.m1, lt2 = m < t.m2, lt3 = m < t.m3;
+    t.nb1 = lt1 ? nb : t.nb1;
+    t.m4 = lt3 ? t.m3 : m;
+    t.m3 = lt2 ? t.m2 : (lt3 ? m : t.m3);
+    t.k3 = lt2 ? t.k2 : (lt3 ? k : t.k3);
+    t.m2 = lt1 ? t.m1 : (lt2 ? m : t.m2);
+    t.k2 = lt1 ? t.k1 : (lt2 ? k : t.k2);
+    t.m1 = lt1 ? m : t.m1;
+    t.k1 = lt1 ? k : t.k1;
+}
+
+// Full facet passes for the lanes with `need`, warp-cooperatively: a group of
+// FG lanes takes one walker, splits its cell's facet list (coalesced loads,
+// FU per lane in flight), merges the per-lane four smallest margins in
+// log2(FG) butterfly rounds and decides as facet_label; the group's first lane
+// writes that walker's label cache.  A walker whose point lies across a facet
+// is queued again from the cell beyond the most violated facet (at most three
+// moves).  Called by all 32 lanes; `start` is each walker's first cell.
+// Returns FACET_IN / FACET_OUT with cell_q set, or a negative code when the
+// voxel-grid classifier has to decide.
+constexpr int FG = 4;
+constexpr int FU = 8;
+
+template <bool PERIODIC>
+MADI_DEV int coop_facets(const Geo& g, const TileShared& ts, bool need, float qx, float qy, float qz, int start,
+                         int lane, int& cell_q) {
+    const int gid = lane / FG, sub = lane % FG;
+    const int warp0 = threadIdx.x & ~31;
+    const int S = g.fstride;
+    int my_cell = start, hops = 0, r_mine = FACET_BAND;
+    bool pend = need;
+    unsigned pending = __ballot_sync(MADI_FULL, pend);
+    while (pending) {
+        const unsigned src = __fns(pending, 0, gid + 1);      // walker of this group, ~0u if none
+        const bool act = src < 32u;
+        const int s = act ? (int)src : 0;
+        const float sx = __shfl_sync(MADI_FULL, qx, s);
+        const float sy = __shfl_sync(MADI_FULL, qy, s);
+        const float sz = __shfl_sync(MADI_FULL, qz, s);
+        const int sc = __shfl_sync(MADI_FULL, my_cell, s);
+        FacetTop t;
+        t.m1 = t.m2 = t.m3 = t.m4 = 3.0e38f;
+        t.k1 = t.k2 = t.k3 = 0;
+        t.nb1 = -1;
+        t.cc = make_float4(0.f, 0.f, 0.f, 0.f);
+        t.wx = t.wy = t.wz = 0.f;
+        if (act) {
+            // the cell record and the cell's facet slots depend only on sc: one
+            // memory round trip for all of them
+            const uint32_t base = (uint32_t)sc * (uint32_t)S;
+            t.cc = g.ccen[sc];
+            for (int k0 = sub; k0 < S; k0 += FG * FU) {
+                float4 f[FU];
+                int nb[FU];
+#pragma unroll
+                for (int i = 0; i < FU; ++i) {
+                    f[i] = g.fpl[base + k0 + FG * i];
+                    nb[i] = g.fnbr[base + k0 + FG * i];
+                }
+                float wx = sx - t.cc.x, wy = sy - t.cc.y, wz = sz - t.cc.z;
+                if (PERIODIC) {
+                    const float hl = 0.5f * g.L;
+                    wx = wx > hl ? wx - g.L : (wx < -hl ? wx + g.L : wx);
+                    wy = wy > hl ? wy - g.L : (wy < -hl ? wy + g.L : wy);
+                    wz = wz > hl ? wz - g.L : (wz < -hl ? wz + g.L : wz);
+                }
+                t.wx = wx; t.wy = wy; t.wz = wz;
+#pragma unroll
+                for (int i = 0; i < FU; ++i) {
+                    const float m = facet_m(f[i], wx, wy, wz);
+                    if (m < t.m4) top4_insert(m, base + k0 + FG * i, nb[i], t);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 1; o < FG; o <<= 1) {
+            const float a1 = __shfl_xor_sync(MADI_FULL, t.m1, o);
+            const float a2 = __shfl_xor_sync(MADI_FULL, t.m2, o);
+            const float a3 = __shfl_xor_sync(MADI_FULL, t.m3, o);
+            const float a4 = __shfl_xor_sync(MADI_FULL, t.m4, o);
+            const uint32_t b1 = __shfl_xor_sync(MADI_FULL, t.k1, o);
+            const uint32_t b2 = __shfl_xor_sync(MADI_FULL, t.k2, o);
+            const uint32_t b3 = __shfl_xor_sync(MADI_FULL, t.k3, o);
+            const int c1 = __shfl_xor_sync(MADI_FULL, t.nb1, o);
+            // only a1 can become the smallest, so only it carries a neighbour
+            if (a1 < t.m4) top4_insert(a1, b1, c1, t);
+            if (a2 < t.m4) top4_insert(a2, b2, -1, t);
+            if (a3 < t.m4) top4_insert(a3, b3, -1, t);
+            t.m4 = fminf(t.m4, a4);
+        }
+        int r = FACET_BAND, nb = -1;
+        if (act) {
+            t.T = fmaf(2.0f * MADI_EPS21, fabsf(t.wx) + fabsf(t.wy) + fabsf(t.wz), g.ftol);
+            if (t.m1 > t.T) {
+                const float dd = t.m1 - t.cc.w;
+                r = dd > t.T ? FACET_IN : (dd < -t.T ? FACET_OUT : FACET_BAND);
+            } else if (t.m1 < -t.T) {
+                r = FACET_LEFT;
+                nb = t.nb1;
+            }
+            if (sub == 0 && r >= 0) fc_build(ts, warp0 + s, t, sc, g.L, g);
+        }
+        // each pending walker reads its group's verdict (group = its rank among the pending)
+        const int rank = __popc(pending & ((1u << lane) - 1u));
+        const bool mine = pend && rank < 32 / FG;
+        const int leader = (mine ? rank : 0) * FG;
+        const int rl = __shfl_sync(MADI_FULL, r, leader);
+        const int nbl = __shfl_sync(MADI_FULL, nb, leader);
+        if (mine) {
+            if (rl == FACET_LEFT && nbl >= 0 && hops < 3) { my_cell = nbl; ++hops; }
+            else { r_mine = rl; pend = false; }
+        }
+        pending = __ballot_sync(MADI_FULL, pend);
+    }
+    __syncwarp();
+    cell_q = my_cell;
+    return r_mine;
+}
 
 // Walk one tile (blockDim.x walkers of one job) on geometry view g.
 template <int OUT, bool PERIODIC, int NP>
@@ -94,6 +246,10 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
     for (int k = 0; k < 3; ++k) { AUX_Y(k) = 0.0; AUX_A(k) = 0.f; AUX_C(k) = 0u; }
 #pragma unroll
     for (int p = 0; p < NP; ++p) { AUX_M(p, 0) = 0.f; AUX_M(p, 1) = 0.f; AUX_M(p, 2) = 0.f; }
+    FC(0) = make_float4(0.f, 0.f, 0.f, 3.0e38f);  // empty label cache
+    FC(3) = make_float4(0.f, 0.f, 0.f, 0.f);
+    FC(4) = make_float4(0.f, 0.f, 0.f, 0.f);
+    FC(5) = make_float4(0.f, 0.f, __int_as_float(-1), __int_as_float(-1));
     if (cells) {
         int my_st = CLS_OK, my_s1 = 0, my_in = 0;
         for (unsigned pend = __ballot_sync(MADI_FULL, active); pend; pend &= pend - 1) {
@@ -185,9 +341,36 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
         // ---- label from the facet planes of the current cell (and its neighbours) ----
         bool t1 = false;
         int t1_in = 0, t1_cell = cell;
+        int start = cell;
         if (ok && facets) {
-            const int r = facet_walk<PERIODIC>(g, qx, qy, qz, cell, t1_cell);
-            if (r >= 0) { t1 = true; t1_in = r; }
+            // inside the cached sphere three planes decide
+            const float4 sp = FC(3), ce = FC(4), f1 = FC(0), th = FC(5);
+            float wx = qx - ce.x, wy = qy - ce.y, wz = qz - ce.z;
+            if (PERIODIC) {
+                const float hl = 0.5f * L;
+                wx = wx > hl ? wx - L : (wx < -hl ? wx + L : wx);
+                wy = wy > hl ? wy - L : (wy < -hl ? wy + L : wy);
+                wz = wz > hl ? wz - L : (wz < -hl ? wz + L : wz);
+            }
+            const float m1 = facet_m(f1, wx, wy, wz);
+            const float ux = wx - sp.x, uy = wy - sp.y, uz = wz - sp.z;
+            if (fmaf(ux, ux, fmaf(uy, uy, uz * uz)) < sp.w) {
+                const float4 f2 = FC(1), f3 = FC(2);
+                const float mm = fminf(m1, fminf(facet_m(f2, wx, wy, wz), facet_m(f3, wx, wy, wz)));
+                if (mm > ce.w) { t1 = true; t1_in = 1; t1_cell = __float_as_int(th.z); }
+                else if (mm > th.y && mm < th.x) { t1 = true; t1_in = 0; t1_cell = __float_as_int(th.z); }
+            }
+            // across the cached cell's nearest facet (an exact plane of it): start
+            // the full pass in the cell beyond
+            const int nb1 = __float_as_int(th.w);
+            if (!t1 && m1 < -th.y && nb1 >= 0) start = nb1;
+        }
+        // ---- cache misses: cooperative full facet passes, which rebuild the caches ----
+        const bool miss = ok && facets && !t1;
+        if (__any_sync(MADI_FULL, miss)) {
+            int cq = start;
+            const int r = coop_facets<PERIODIC>(g, ts, miss, qx, qy, qz, start, lane, cq);
+            if (miss && r >= 0) { t1 = true; t1_in = r; t1_cell = cq; }
         }
         // ---- full classifications of this step, one warp-cooperative pass each ----
         const bool need = ok && cells && !t1;
@@ -363,7 +546,8 @@ __global__ void __launch_bounds__(256, MINB) walk_f32_kernel(const madi_walk_des
     ts.snap = snap;
     unsigned char* aux = smem + d.stage_smem + 16 * n_out + 12 * ((d.n_grid + 3) & ~3);
     ts.auxd = reinterpret_cast<double*>(aux);
-    ts.auxf = reinterpret_cast<float*>(aux + 24 * nthr);
+    ts.fc = reinterpret_cast<float4*>(aux + 24 * nthr);
+    ts.auxf = reinterpret_cast<float*>(aux + (24 + FC_BYTES_PER_WALKER) * nthr);
     ts.auxc = reinterpret_cast<uint32_t*>(ts.auxf + (3 + 3 * NP) * nthr);
 
     for (int j = tid; j < d.n_grid; j += nthr) {
@@ -574,7 +758,7 @@ extern "C" int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walker
 static int64_t fused_smem(const madi_walk_desc* d, int np) {
     const int64_t n_out = (int64_t)d->n_pairs * d->n_b * d->n_dirs;
     return (int64_t)d->stage_smem + 16ll * n_out + 12ll * ((d->n_grid + 3) & ~3) +
-           (24 + 4 * (3 + 3 * np) + 12) * d->tile_walkers;
+           (24 + FC_BYTES_PER_WALKER + 4 * (3 + 3 * np) + 12) * d->tile_walkers;
 }
 
 template <int OUT, bool PER, int NP, int MINB>

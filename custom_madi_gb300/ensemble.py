@@ -400,15 +400,27 @@ class DeviceGeometry:
         # facet table of the base cells (periodic: the first n_cells seeds, images generated natively)
         periodic = ens.boundary_mode == "periodic"
         if ens.is_free_water:
-            n_cells, centers, fbeg = 0, np.zeros((0, 4), np.float32), np.zeros(1, np.uint32)
+            n_cells, centers, self.facet_stride = 0, np.zeros((0, 4), np.float32), 0
             fpl, fnbr, h_max = np.zeros((0, 4), np.float32), np.zeros(0, np.int32), 0.0
         else:
             n_cells = int(cellid.max()) + 1
             base = xyza[:n_cells]
             if not np.array_equal(cellid[:n_cells], np.arange(n_cells)):
                 raise RuntimeError("classifier seeds must list the base cells first")
-            fbeg, fpl, fnbr, h_max, self.facet_reach = build_facets(base, periodic, float(ens.L))
+            fbeg, fpl_csr, fnbr_csr, h_max, self.facet_reach = build_facets(base, periodic, float(ens.L))
             centers = base.astype(np.float32)
+            # fixed stride per cell (a multiple of 32): the walker loads a cell's
+            # slots without first reading where they start
+            cnt = np.diff(fbeg.astype(np.int64))
+            stride = int(max(32, -(-int(cnt.max()) // 32) * 32))
+            fpl = np.zeros((n_cells, stride, 4), np.float32)
+            fpl[:, :, 3] = 3.0e38
+            fnbr = np.full((n_cells, stride), -1, np.int32)
+            slot = np.arange(len(fnbr_csr)) - np.repeat(fbeg[:-1].astype(np.int64), cnt)
+            row = np.repeat(np.arange(n_cells), cnt)
+            fpl[row, slot] = fpl_csr
+            fnbr[row, slot] = fnbr_csr
+            self.facet_stride = stride
         self.n_cells = n_cells
         self.facets_mean = float(np.count_nonzero(fnbr >= 0)) / max(n_cells, 1)
         # |m - m_exact| <= 2 e + 2^-21 (h + |w|_1 + L) for fp32 facet margins, taken twice
@@ -419,7 +431,7 @@ class DeviceGeometry:
             return b + b"\0" * ((-len(b)) % 16)
 
         parts = [hi.tobytes(), pad16(cellid.tobytes()), pad16(offsets.tobytes()), pad16(ids.tobytes()),
-                 pad16(centers.tobytes()), pad16(fbeg.tobytes()), pad16(fpl.tobytes()), pad16(fnbr.tobytes())]
+                 pad16(centers.tobytes()), pad16(fpl.tobytes()), pad16(fnbr.tobytes())]
         offs = np.cumsum([0] + [len(p) for p in parts])
         off_cell, off_go, off_gi = int(offs[1]), int(offs[2]), int(offs[3])
         blob = b"".join(parts)
@@ -446,7 +458,8 @@ class DeviceGeometry:
         s.source_lo = float(ens.source_lo)
         s.source_hi = float(ens.source_hi)
         s.coord_err = self.coord_err
-        s.off_cell_center, s.off_facet_begin, s.off_facet_plane, s.off_facet_nbr = (int(o) for o in offs[4:8])
+        s.off_cell_center, s.off_facet_plane, s.off_facet_nbr = (int(o) for o in offs[4:7])
+        s.facet_stride = self.facet_stride
         s.n_cells = n_cells
         s.facet_tol = self.facet_tol
         self.struct = s

@@ -34,6 +34,9 @@ except Exception:  # pragma: no cover - torch is a hard dependency in practice
 PAPER_WALKS_PER_ENTRY = PRODUCTION_AXIS_WALKS_PER_ENTRY
 PHILOX_KEY1 = 0x4D414449  # "MADI": second Philox key word, fixed
 FIXED_POINT_SCALE = 2.0 ** 32
+# Per-walker label cache in the walker's shared memory (six float4); the
+# kernel's layout uses the same figure.
+FC_BYTES_PER_WALKER = 6 * 16
 
 
 def pp_to_kio_eq5(pp: float, mean_AV: float, cfg: SimConfig) -> float:
@@ -360,7 +363,7 @@ class WalkBatch:
         # shared-memory staging (every geometry that fits the per-CTA budget) and persistent grid
         budget = lc.stage_budget if lc.staged is not False else 0
         np_ = 8 if (layout is not None and layout.n_pairs > 4) else 4
-        fused_extra = 16 * self.n_out + 12 * ((cfg.n_grid + 3) // 4 * 4) + (24 + 4 * (3 + 3 * np_) + 12) * tw
+        fused_extra = 16 * self.n_out + 12 * ((cfg.n_grid + 3) // 4 * 4) + (24 + FC_BYTES_PER_WALKER + 4 * (3 + 3 * np_) + 12) * tw
         fits = [g.stage_bytes for g in geoms if g.stage_bytes + fused_extra <= min(budget, 227 * 1024)]
         d.stage_smem = ((max(fits) + 15) // 16 * 16) if (fits and precision == 32) else 0
         self.smem_bytes = d.stage_smem + fused_extra

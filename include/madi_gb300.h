@@ -87,12 +87,14 @@ typedef struct madi_geometry {
     double   source_lo;            /* walkers start uniform in [lo, hi)^3         */
     double   source_hi;
     double   coord_err;            /* bound on |fp32 seed - fp64 seed| per axis   */
-    /* Cell facet table (madi_facets_build), byte offsets inside stage.  With
-     * n_cells = 0 the walker labels every step with the voxel-grid classifier. */
+    /* Cell facet table (madi_facets_build), byte offsets inside stage; cell c
+     * owns slots c * facet_stride .. + facet_stride - 1, unused slots hold
+     * (0, 0, 0, 3e38) and neighbour -1.  With n_cells = 0 the walker labels
+     * every step with the voxel-grid classifier. */
     uint32_t off_cell_center;      /* float4 [n_cells]: base seed x, y, z, alpha  */
-    uint32_t off_facet_begin;      /* uint32 [n_cells + 1]: facet range per cell  */
-    uint32_t off_facet_plane;      /* float4 [n_facets]: unit normal n, offset h  */
-    uint32_t off_facet_nbr;        /* int32 [n_facets]: cell across the facet     */
+    uint32_t facet_stride;         /* facet slots per cell, a multiple of 32      */
+    uint32_t off_facet_plane;      /* float4 [n_cells][facet_stride]: n, offset h */
+    uint32_t off_facet_nbr;        /* int32 [n_cells][facet_stride]: cell across  */
     int32_t  n_cells;              /* cells in the table (0 = no table)           */
     int32_t  pad1;
     double   facet_tol;            /* fp32 error of h - n.w, without the |w| term */
