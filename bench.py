@@ -31,6 +31,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "walker-steps/s"
 CONFIG_NAME = "batched library build: 256 entries x 1e5 walkers x 4600 steps, 27-512 cells, 20 cols x 24 dirs"
+# walk_f32_kernel DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum)
+# per walker-step, from one ncu capture of 16 entries x 2e4 walkers x 4,600
+# steps: 6.40 MB + 0.14 MB over 1.472e9 walker-steps
+WALK_DRAM_BYTES_PER_WALKER_STEP = 6.54e6 / 1.472e9
 
 
 def _dist():
@@ -252,17 +256,18 @@ def main(argv=None):
     n_ws = max(int(counters[0]) * cfg.n_steps, 1)
     f_full = counters[3] / n_ws
     f_t1 = counters[4] / n_ws
+    f_fp = counters[8] / n_ws
     k_mean = float(np.average([g.candidates_mean for g in batch.geoms]))
-    ops_step = 255.0 + f_full * 25.0 * k_mean + f_t1 * 12.0
+    nf_mean = float(np.average([g.facets_mean for g in batch.geoms]))
+    # 255 RNG + move + Y, 34 label-cache test (sphere, three planes), 6 per facet
+    # of a full facet pass, 25 per candidate of a voxel-grid pass
+    ops_step = 255.0 + 34.0 + f_fp * 6.0 * nf_mean + f_full * 25.0 * k_mean
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     peak_ops = sm_count * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
     achieved = (steps_per_run * args.steps / dev_s) * ops_step / 1e12
-    traffic = None
-    tp = ROOT / "profiles" / "walk_f32_traffic.json"
-    if tp.exists():
-        per_ws = json.loads(tp.read_text()).get("dram_bytes_per_walker_step")
-        if per_ws is not None:
-            traffic = float(per_ws) * steps_per_run
+    # DRAM bytes per launch: the ncu capture of the 16-entry case (6.54 MB for
+    # 1.47e9 walker-steps) scaled by walker-steps
+    traffic = WALK_DRAM_BYTES_PER_WALKER_STEP * steps_per_run
     line = {
         "metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_s / args.steps * 1e3, "higher_is_better": True,
@@ -274,15 +279,17 @@ def main(argv=None):
                    "launch": "one CUDA graph replay per step (zeroing + persistent walk)"},
         "roofline": {"bound": "issue", "achieved": achieved, "peak": peak_ops, "unit": "Top/s",
                      "frac": achieved / peak_ops, "traffic": traffic,
-                     "note": f"lane-ops per walker-step {ops_step:.1f} (255 RNG+move, 25 x {k_mean:.1f} candidates "
-                             f"x {f_full:.3f} full classifications, 12 x {f_t1:.3f} Tier-1); peak = SMs x 128 lanes x "
-                             f"sm_max_mhz ({peak_kind} clock)"},
+                     "note": f"lane-ops per walker-step {ops_step:.1f} (255 RNG+move+Y, 34 label-cache test, "
+                             f"6 x {nf_mean:.1f} facets x {f_fp:.3f} facet passes, 25 x {k_mean:.1f} candidates x "
+                             f"{f_full:.4f} voxel-grid passes); peak = SMs x 128 lanes x sm_max_mhz ({peak_kind} clock); "
+                             f"traffic scaled from the 16-entry ncu capture"},
         "e2e": {"value": e2e_val, "unit": "walker-steps/s", "h2d_bytes_per_step": int(host["h2d_bytes"]),
                 "d2h_bytes_per_step": int(host["d2h_bytes"])},
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
         "staged_fraction": batch.staged_fraction,
         "walker_counters": {"full_per_step": float(f_full), "tier1_per_step": float(f_t1),
+                            "facet_pass_per_step": float(f_fp),
                             "fallback64": int(counters[5]), "escaped": int(counters[1]),
                             "classifier_error": int(counters[2])},
         "host_ensemble_build_s": t_build,

@@ -37,7 +37,7 @@ MADI_MATCH_FP32 = 0
 MADI_MATCH_BF16 = 1
 
 CNT_NAMES = ("walkers", "escaped", "classifier_error", "full", "tier1", "fallback64",
-             "cross_accept", "cross_reject")
+             "cross_accept", "cross_reject", "facet_pass")
 MADI_CNT_N = len(CNT_NAMES)
 
 EXPORTED = (

@@ -241,7 +241,7 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
     const bool facets = cells && g.n_cells > 0;
     bool dead = !active;
     bool frozen = !active;
-    uint32_t n_full = 0, n_t1 = 0, escaped = 0, cerr = 0;
+    uint32_t n_full = 0, n_t1 = 0, n_fp = 0, escaped = 0, cerr = 0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) { AUX_Y(k) = 0.0; AUX_A(k) = 0.f; AUX_C(k) = 0u; }
 #pragma unroll
@@ -367,6 +367,7 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
         }
         // ---- cache misses: cooperative full facet passes, which rebuild the caches ----
         const bool miss = ok && facets && !t1;
+        n_fp += miss ? 1u : 0u;
         if (__any_sync(MADI_FULL, miss)) {
             int cq = start;
             const int r = coop_facets<PERIODIC>(g, ts, miss, qx, qy, qz, start, lane, cq);
@@ -516,6 +517,7 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
         const uint32_t v5 = __reduce_add_sync(0xffffffffu, AUX_C(0));
         const uint32_t v6 = __reduce_add_sync(0xffffffffu, AUX_C(1));
         const uint32_t v7 = __reduce_add_sync(0xffffffffu, AUX_C(2));
+        const uint32_t v8 = __reduce_add_sync(0xffffffffu, n_fp);
         if (lane == 0) {
             unsigned long long* c = reinterpret_cast<unsigned long long*>(cnt);
             if (v0) atomicAdd(&c[0], (unsigned long long)v0);
@@ -526,6 +528,7 @@ __device__ __forceinline__ void walk_tile(const madi_walk_desc& d, const madi_wa
             if (v5) atomicAdd(&c[5], (unsigned long long)v5);
             if (v6) atomicAdd(&c[6], (unsigned long long)v6);
             if (v7) atomicAdd(&c[7], (unsigned long long)v7);
+            if (v8) atomicAdd(&c[MADI_CNT_FACET_PASS], (unsigned long long)v8);
         }
     }
 }

@@ -139,11 +139,14 @@ typedef struct madi_walk_job {
     uint64_t thr2;            /* floor(pp^2 * 2^64)                                  */
 } madi_walk_job;
 
-/* Device counters per slot (uint64 each), zeroed by the caller. */
+/* Device counters per slot (uint64 each), zeroed by the caller.  FULL:
+ * voxel-grid classifications; TIER1: steps labelled from facet planes (label
+ * cache or full facet pass); FALLBACK64: fp64 decisions; FACET_PASS: full
+ * facet passes (label cache misses). */
 enum {
     MADI_CNT_WALKERS = 0, MADI_CNT_ESCAPED, MADI_CNT_CLASSIFIER_ERROR,
     MADI_CNT_FULL, MADI_CNT_TIER1, MADI_CNT_FALLBACK64, MADI_CNT_CROSS_ACCEPT,
-    MADI_CNT_CROSS_REJECT, MADI_CNT_N
+    MADI_CNT_CROSS_REJECT, MADI_CNT_FACET_PASS, MADI_CNT_N
 };
 
 /*
