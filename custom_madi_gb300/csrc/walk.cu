@@ -78,29 +78,54 @@ MADI_DEV void fc_build(const TileShared& ts, int w, const FacetTop& t, int c, fl
     f[5 * n] = make_float4(t.cc.w - Tm, Tm, __int_as_float(c), __int_as_float(t.nb1));
 }
 
-// (m1, k1) <= (m2, k2) <= (m3, k3) <= m4 after adding margin m of facet slot
-// k with neighbour nb (m < m4); nb1 follows k1.
-MADI_DEV void top4_insert(float m, uint32_t k, int nb, FacetTop& t) {
-    const bool lt1 = m < t.m1, lt2 = m < t.m2, lt3 = m < t.m3;
-    t.nb1 = lt1 ? nb : t.nb1;
-    t.m4 = lt3 ? t.m3 : m;
-    t.m3 = lt2 ? t.m2 : (lt3 ? m : t.m3);
-    t.k3 = lt2 ? t.k2 : (lt3 ? k : t.k3);
-    t.m2 = lt1 ? t.m1 : (lt2 ? m : t.m2);
-    t.k2 = lt1 ? t.k1 : (lt2 ? k : t.k2);
-    t.m1 = lt1 ? m : t.m1;
-    t.k1 = lt1 ? k : t.k1;
+// Order-preserving 32-bit key of a facet margin: the float's bits mapped to
+// unsigned order, the low KEY_BITS replaced by the facet's slot.  Dropping
+// those mantissa bits rounds the margin down (towards -inf) by at most
+// 2^(KEY_BITS - 23) relative; key_floor() returns that lower bound.
+constexpr int KEY_BITS = 6;                      // slots per cell <= 64
+constexpr uint32_t KEY_SLOT = (1u << KEY_BITS) - 1u;
+
+MADI_DEV uint32_t margin_key(float m, uint32_t slot) {
+    const uint32_t b = __float_as_uint(m);
+    const uint32_t u = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    return (u & ~KEY_SLOT) | slot;
+}
+
+MADI_DEV float key_floor(uint32_t key) {
+    const uint32_t u = key & ~KEY_SLOT;
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+MADI_DEV void cx(uint32_t& a, uint32_t& b) {
+    const uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo; b = hi;
+}
+
+// ascending sort of four keys
+MADI_DEV void sort4(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d) {
+    cx(a, b); cx(c, d); cx(a, c); cx(b, d); cx(b, c);
+}
+
+// the four smallest of two ascending quadruples, ascending, into (a0..a3)
+MADI_DEV void merge4(uint32_t& a0, uint32_t& a1, uint32_t& a2, uint32_t& a3, uint32_t b0, uint32_t b1,
+                     uint32_t b2, uint32_t b3) {
+    a0 = min(a0, b3); a1 = min(a1, b2); a2 = min(a2, b1); a3 = min(a3, b0);   // bitonic
+    cx(a0, a2); cx(a1, a3); cx(a0, a1); cx(a2, a3);
 }
 
 // Full facet passes for the lanes with `need`, warp-cooperatively: a group of
-// FG lanes takes one walker, splits its cell's facet list (coalesced loads,
-// FU per lane in flight), merges the per-lane four smallest margins in
-// log2(FG) butterfly rounds and decides as facet_label; the group's first lane
-// writes that walker's label cache.  A walker whose point lies across a facet
-// is queued again from the cell beyond the most violated facet (at most three
-// moves).  Called by all 32 lanes; `start` is each walker's first cell.
-// Returns FACET_IN / FACET_OUT with cell_q set, or a negative code when the
-// voxel-grid classifier has to decide.
+// FG lanes takes one walker, splits its cell's facet slots (FU loads per lane
+// in flight, coalesced), keeps each lane's four smallest margin keys with
+// sorting networks and merges the group's in log2(FG) butterfly rounds.  The
+// three smallest keys name the cached facets, whose margins are recomputed
+// exactly (the true smallest margin is among them unless four margins lie
+// within 2^-17 relative of each other, which the widened band covers); the
+// fourth key bounds every other facet from below.  The group decides as
+// facet_label and its first lane writes the walker's label cache.  A walker
+// whose point lies across a facet is queued again from the cell beyond the
+// most violated facet (at most three moves).  Called by all 32 lanes; `start`
+// is each walker's first cell.  Returns FACET_IN / FACET_OUT with cell_q
+// set, or a negative code when the voxel-grid classifier has to decide.
 constexpr int FG = 4;
 constexpr int FU = 8;
 
@@ -121,63 +146,61 @@ MADI_DEV int coop_facets(const Geo& g, const TileShared& ts, bool need, float qx
         const float sy = __shfl_sync(MADI_FULL, qy, s);
         const float sz = __shfl_sync(MADI_FULL, qz, s);
         const int sc = __shfl_sync(MADI_FULL, my_cell, s);
-        FacetTop t;
-        t.m1 = t.m2 = t.m3 = t.m4 = 3.0e38f;
-        t.k1 = t.k2 = t.k3 = 0;
-        t.nb1 = -1;
-        t.cc = make_float4(0.f, 0.f, 0.f, 0.f);
-        t.wx = t.wy = t.wz = 0.f;
+        const uint32_t base = (uint32_t)sc * (uint32_t)S;
+        float4 cc = make_float4(0.f, 0.f, 0.f, 0.f);
+        float wx = 0.f, wy = 0.f, wz = 0.f;
+        uint32_t q0 = 0xffffffffu, q1 = 0xffffffffu, q2 = 0xffffffffu, q3 = 0xffffffffu;
         if (act) {
-            // the cell record and the cell's facet slots depend only on sc: one
-            // memory round trip for all of them
-            const uint32_t base = (uint32_t)sc * (uint32_t)S;
-            t.cc = g.ccen[sc];
+            // the cell record and the cell's slots depend only on sc: one round trip
+            cc = g.ccen[sc];
             for (int k0 = sub; k0 < S; k0 += FG * FU) {
                 float4 f[FU];
-                int nb[FU];
 #pragma unroll
-                for (int i = 0; i < FU; ++i) {
-                    f[i] = g.fpl[base + k0 + FG * i];
-                    nb[i] = g.fnbr[base + k0 + FG * i];
-                }
-                float wx = sx - t.cc.x, wy = sy - t.cc.y, wz = sz - t.cc.z;
+                for (int i = 0; i < FU; ++i) f[i] = g.fpl[base + k0 + FG * i];
+                wx = sx - cc.x; wy = sy - cc.y; wz = sz - cc.z;
                 if (PERIODIC) {
                     const float hl = 0.5f * g.L;
                     wx = wx > hl ? wx - g.L : (wx < -hl ? wx + g.L : wx);
                     wy = wy > hl ? wy - g.L : (wy < -hl ? wy + g.L : wy);
                     wz = wz > hl ? wz - g.L : (wz < -hl ? wz + g.L : wz);
                 }
-                t.wx = wx; t.wy = wy; t.wz = wz;
+                uint32_t k[FU];
 #pragma unroll
-                for (int i = 0; i < FU; ++i) {
-                    const float m = facet_m(f[i], wx, wy, wz);
-                    if (m < t.m4) top4_insert(m, base + k0 + FG * i, nb[i], t);
-                }
+                for (int i = 0; i < FU; ++i) k[i] = margin_key(facet_m(f[i], wx, wy, wz), (uint32_t)(k0 + FG * i));
+                sort4(k[0], k[1], k[2], k[3]);
+                sort4(k[4], k[5], k[6], k[7]);
+                merge4(k[0], k[1], k[2], k[3], k[4], k[5], k[6], k[7]);
+                merge4(q0, q1, q2, q3, k[0], k[1], k[2], k[3]);
             }
         }
 #pragma unroll
         for (int o = 1; o < FG; o <<= 1) {
-            const float a1 = __shfl_xor_sync(MADI_FULL, t.m1, o);
-            const float a2 = __shfl_xor_sync(MADI_FULL, t.m2, o);
-            const float a3 = __shfl_xor_sync(MADI_FULL, t.m3, o);
-            const float a4 = __shfl_xor_sync(MADI_FULL, t.m4, o);
-            const uint32_t b1 = __shfl_xor_sync(MADI_FULL, t.k1, o);
-            const uint32_t b2 = __shfl_xor_sync(MADI_FULL, t.k2, o);
-            const uint32_t b3 = __shfl_xor_sync(MADI_FULL, t.k3, o);
-            const int c1 = __shfl_xor_sync(MADI_FULL, t.nb1, o);
-            // only a1 can become the smallest, so only it carries a neighbour
-            if (a1 < t.m4) top4_insert(a1, b1, c1, t);
-            if (a2 < t.m4) top4_insert(a2, b2, -1, t);
-            if (a3 < t.m4) top4_insert(a3, b3, -1, t);
-            t.m4 = fminf(t.m4, a4);
+            const uint32_t b0 = __shfl_xor_sync(MADI_FULL, q0, o);
+            const uint32_t b1 = __shfl_xor_sync(MADI_FULL, q1, o);
+            const uint32_t b2 = __shfl_xor_sync(MADI_FULL, q2, o);
+            const uint32_t b3 = __shfl_xor_sync(MADI_FULL, q3, o);
+            merge4(q0, q1, q2, q3, b0, b1, b2, b3);
         }
         int r = FACET_BAND, nb = -1;
         if (act) {
-            t.T = fmaf(2.0f * MADI_EPS21, fabsf(t.wx) + fabsf(t.wy) + fabsf(t.wz), g.ftol);
-            if (t.m1 > t.T) {
-                const float dd = t.m1 - t.cc.w;
+            FacetTop t;
+            t.k1 = base + (q0 & KEY_SLOT);
+            t.k2 = base + (q1 & KEY_SLOT);
+            t.k3 = base + (q2 & KEY_SLOT);
+            t.m4 = key_floor(q3);
+            const float e1 = facet_m(g.fpl[t.k1], wx, wy, wz);
+            const float e2 = facet_m(g.fpl[t.k2], wx, wy, wz);
+            const float e3 = facet_m(g.fpl[t.k3], wx, wy, wz);
+            const uint32_t kmin = e1 <= e2 ? (e1 <= e3 ? t.k1 : t.k3) : (e2 <= e3 ? t.k2 : t.k3);
+            const float m1 = fminf(e1, fminf(e2, e3));
+            t.m1 = m1;
+            t.wx = wx; t.wy = wy; t.wz = wz; t.cc = cc;
+            t.T = fmaf(2.0f * MADI_EPS21, fabsf(wx) + fabsf(wy) + fabsf(wz), g.ftol) + 7.62939453125e-6f * fabsf(m1);
+            t.nb1 = g.fnbr[kmin];
+            if (m1 > t.T) {
+                const float dd = m1 - cc.w;
                 r = dd > t.T ? FACET_IN : (dd < -t.T ? FACET_OUT : FACET_BAND);
-            } else if (t.m1 < -t.T) {
+            } else if (m1 < -t.T) {
                 r = FACET_LEFT;
                 nb = t.nb1;
             }

@@ -413,11 +413,18 @@ class DeviceGeometry:
             # slots without first reading where they start
             cnt = np.diff(fbeg.astype(np.int64))
             stride = int(max(32, -(-int(cnt.max()) // 32) * 32))
+            if stride > 64:
+                # margin keys carry the slot in 6 bits; a cell with more than 64
+                # facets (never met with Poisson seeds) leaves the walker on the
+                # voxel-grid classifier for this geometry
+                n_cells, stride = 0, 32
+                cnt = np.zeros_like(cnt)
+                fpl_csr, fnbr_csr = fpl_csr[:0], fnbr_csr[:0]
             fpl = np.zeros((n_cells, stride, 4), np.float32)
             fpl[:, :, 3] = 3.0e38
             fnbr = np.full((n_cells, stride), -1, np.int32)
             slot = np.arange(len(fnbr_csr)) - np.repeat(fbeg[:-1].astype(np.int64), cnt)
-            row = np.repeat(np.arange(n_cells), cnt)
+            row = np.repeat(np.arange(len(cnt)), cnt)
             fpl[row, slot] = fpl_csr
             fnbr[row, slot] = fnbr_csr
             self.facet_stride = stride
