@@ -64,15 +64,17 @@ struct TileShared {
 // the facet crossed.
 constexpr int FC_BYTES_PER_WALKER = 6 * 16;
 
-// Writes the cache of the walker in thread `w` (this CTA) from a full pass.
-MADI_DEV void fc_build(const TileShared& ts, int w, const FacetTop& t, int c, float L, const Geo& g) {
+// Writes the cache of the walker in thread `w` (this CTA) from a full pass;
+// p1..p3 are the records of facets k1..k3.
+MADI_DEV void fc_build(const TileShared& ts, int w, const FacetTop& t, int c, float L, const float4& p1,
+                       const float4& p2, const float4& p3) {
     const float Tm = 3.0f * t.T;
     const float R = fminf(t.m4 - t.cc.w - 8.0f * t.T, L);
     float4* f = ts.fc + w;
     const int n = blockDim.x;
-    f[0] = g.fpl[t.k1];
-    f[n] = g.fpl[t.k2];
-    f[2 * n] = g.fpl[t.k3];
+    f[0] = p1;
+    f[n] = p2;
+    f[2 * n] = p3;
     f[3 * n] = make_float4(t.wx, t.wy, t.wz, R > 0.f ? R * R * (1.0f - MADI_EPS19) : 0.f);
     f[4 * n] = make_float4(t.cc.x, t.cc.y, t.cc.z, t.cc.w + Tm);
     f[5 * n] = make_float4(t.cc.w - Tm, Tm, __int_as_float(c), __int_as_float(t.nb1));
@@ -188,15 +190,17 @@ MADI_DEV int coop_facets(const Geo& g, const TileShared& ts, bool need, float qx
             t.k2 = base + (q1 & KEY_SLOT);
             t.k3 = base + (q2 & KEY_SLOT);
             t.m4 = key_floor(q3);
-            const float e1 = facet_m(g.fpl[t.k1], wx, wy, wz);
-            const float e2 = facet_m(g.fpl[t.k2], wx, wy, wz);
-            const float e3 = facet_m(g.fpl[t.k3], wx, wy, wz);
-            const uint32_t kmin = e1 <= e2 ? (e1 <= e3 ? t.k1 : t.k3) : (e2 <= e3 ? t.k2 : t.k3);
+            // the three candidates' records and neighbours, loaded together (L1)
+            const float4 p1 = g.fpl[t.k1], p2 = g.fpl[t.k2], p3 = g.fpl[t.k3];
+            const int n1 = g.fnbr[t.k1], n2 = g.fnbr[t.k2], n3 = g.fnbr[t.k3];
+            const float e1 = facet_m(p1, wx, wy, wz);
+            const float e2 = facet_m(p2, wx, wy, wz);
+            const float e3 = facet_m(p3, wx, wy, wz);
             const float m1 = fminf(e1, fminf(e2, e3));
             t.m1 = m1;
             t.wx = wx; t.wy = wy; t.wz = wz; t.cc = cc;
             t.T = fmaf(2.0f * MADI_EPS21, fabsf(wx) + fabsf(wy) + fabsf(wz), g.ftol) + 7.62939453125e-6f * fabsf(m1);
-            t.nb1 = g.fnbr[kmin];
+            t.nb1 = e1 <= e2 ? (e1 <= e3 ? n1 : n3) : (e2 <= e3 ? n2 : n3);
             if (m1 > t.T) {
                 const float dd = m1 - cc.w;
                 r = dd > t.T ? FACET_IN : (dd < -t.T ? FACET_OUT : FACET_BAND);
@@ -204,7 +208,7 @@ MADI_DEV int coop_facets(const Geo& g, const TileShared& ts, bool need, float qx
                 r = FACET_LEFT;
                 nb = t.nb1;
             }
-            if (sub == 0 && r >= 0) fc_build(ts, warp0 + s, t, sc, g.L, g);
+            if (sub == 0 && r >= 0) fc_build(ts, warp0 + s, t, sc, g.L, p1, p2, p3);
         }
         // each pending walker reads its group's verdict (group = its rank among the pending)
         const int rank = __popc(pending & ((1u << lane) - 1u));
