@@ -134,13 +134,13 @@ def cpu_walk_rate(ensembles, jobs, cfg, dirs, budget_s: float, threads: int, ste
     return steps / dt, f"{n_entries} of the entries x {per} walkers x {cfg.n_steps} steps ({dt:.1f} s)"
 
 
-def build_workload(rank: int, n_entries: int, n_walkers: int, threads: int):
+def build_workload(rank: int, n_entries: int, n_walkers: int, threads: int, measure_vi: bool = True):
     from custom_madi_gb300 import workloads as WL
     from custom_madi_gb300.walker_gpu import WalkJob, kio_to_pp, _walk_seed
     cfg = WL.batch_config(n_walkers=n_walkers)
     trip = WL.batch_triplets(n_entries, seed=1 + 1000 * rank)
     t0 = time.perf_counter()
-    ens = WL.build_ensembles(trip, cfg, seed=1000 * rank, threads=threads)
+    ens = WL.build_ensembles(trip, cfg, seed=1000 * rank, threads=threads, measure_vi=measure_vi)
     t_build = time.perf_counter() - t0
     jobs = [WalkJob(e, kio_to_pp(t[0], e.mean_AV, cfg), _walk_seed(0, 0), n_walkers) for e, t in zip(ens, trip)]
     return cfg, ens, jobs, t_build
@@ -150,7 +150,7 @@ def run_reference_arm(args, ws, rank):
     if rank != 0:
         return 0
     threads = len(os.sched_getaffinity(0))
-    cfg, ens, jobs, _ = build_workload(0, 16, args.walkers, threads)
+    cfg, ens, jobs, _ = build_workload(0, 16, args.walkers, threads, measure_vi=False)   # host only
     dirs = cfg.direction_array()
     rates = []
     for i in range(args.warmup + args.steps):

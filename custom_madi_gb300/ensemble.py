@@ -579,7 +579,8 @@ def _tile_periodic(seeds: np.ndarray, annulus: np.ndarray, L: float, margin: flo
 
 def create_ensemble(rho: float, V: float, cfg: Optional[SimConfig] = None, seed: Optional[int] = None,
                     verbose: bool = False, verify_vi: bool = True, *,
-                    voxel_per_spacing: float = 0.5, cap_per_spacing: float = 0.125) -> Ensemble:
+                    voxel_per_spacing: float = 0.5, cap_per_spacing: float = 0.125,
+                    measure_vi: bool = True) -> Ensemble:
     """Build one ensemble for the requested (rho [cells/uL], V [pL]) (madi/ensemble.py:649-757).
 
     cfg.boundary_mode selects the SI finite domain (fatal escape) or a periodic
@@ -655,7 +656,10 @@ def create_ensemble(rho: float, V: float, cfg: Optional[SimConfig] = None, seed:
         tree=None if periodic else tree, boundary_mode=cfg.boundary_mode,
         classifier_seeds=cs, classifier_annulus=ca, classifier_cell=cc,
         grid_h=h, grid_n=G, safe_cap=cap)
-    realised, se = _measure_vi(ens, cfg.geometry_validation_points, rng)
+    if measure_vi or verify_vi:
+        realised, se = _measure_vi(ens, cfg.geometry_validation_points, rng)
+    else:       # host-only builds (CPU timing legs): v_i left at its target
+        realised, se = float(target_vi), float("nan")
     allowed = max(float(cfg.geometry_vi_tolerance), 4.0 * se)
     if verify_vi and abs(realised - target_vi) > allowed:
         raise RuntimeError(

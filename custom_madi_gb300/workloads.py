@@ -50,14 +50,15 @@ def batch_triplets(n: int = 256, seed: int = 1, vi_lo: float = 0.5, vi_hi: float
     return out
 
 
-def build_ensembles(triplets, cfg: SimConfig, seed: int = 0, threads: int = 8, verify_vi: bool = False):
+def build_ensembles(triplets, cfg: SimConfig, seed: int = 0, threads: int = 8, verify_vi: bool = False,
+                    measure_vi: bool = True):
     """One periodic ensemble per (kio, rho, V, n_cells), built on host threads."""
     from .ensemble import create_ensemble
 
     def one(i_t):
         i, (kio, rho, V, nc) = i_t
         c = replace(cfg, n_cells=int(nc))
-        return create_ensemble(rho, V, c, seed=seed + i, verify_vi=verify_vi)
+        return create_ensemble(rho, V, c, seed=seed + i, verify_vi=verify_vi, measure_vi=measure_vi)
     with ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
         return list(ex.map(one, enumerate(triplets)))
 
