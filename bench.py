@@ -33,8 +33,8 @@ METRIC = "walker-steps/s"
 CONFIG_NAME = "batched library build: 256 entries x 1e5 walkers x 4600 steps, 27-512 cells, 20 cols x 24 dirs"
 # walk_f32_kernel DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum)
 # per walker-step, from one ncu capture of 16 entries x 2e4 walkers x 4,600
-# steps: 6.40 MB + 0.14 MB over 1.472e9 walker-steps
-WALK_DRAM_BYTES_PER_WALKER_STEP = 6.54e6 / 1.472e9
+# steps: 6.39 MB + 0 MB over 1.472e9 walker-steps
+WALK_DRAM_BYTES_PER_WALKER_STEP = 6.39e6 / 1.472e9
 
 
 def _dist():
@@ -265,7 +265,7 @@ def main(argv=None):
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     peak_ops = sm_count * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
     achieved = (steps_per_run * args.steps / dev_s) * ops_step / 1e12
-    # DRAM bytes per launch: the ncu capture of the 16-entry case (6.54 MB for
+    # DRAM bytes per launch: the ncu capture of the 16-entry case (6.39 MB for
     # 1.47e9 walker-steps) scaled by walker-steps
     traffic = WALK_DRAM_BYTES_PER_WALKER_STEP * steps_per_run
     line = {
