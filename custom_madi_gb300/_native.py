@@ -196,6 +196,20 @@ def lib():
     return _lib
 
 
+_lib_digest = None
+
+
+def lib_digest() -> str:
+    """Short hash of the loaded native library's file: tuned launch shapes are
+    keyed on it, so a rebuilt kernel is tuned again."""
+    global _lib_digest
+    if _lib_digest is None:
+        import hashlib
+        lib()
+        _lib_digest = hashlib.sha256(_build.library_path().read_bytes()).hexdigest()[:12]
+    return _lib_digest
+
+
 def check(status: int, what: str) -> None:
     if status == MADI_OK:
         return

@@ -54,7 +54,7 @@ def key_for(jobs: Sequence[WalkJob], layout: PairLayout, n_dirs: int, sm_count: 
     bucket = int(2 ** np.ceil(np.log2(max(seeds, 2))))
     stage = max(j.ensemble.device().stage_bytes for j in jobs)
     sbucket = int(2 ** np.ceil(np.log2(max(stage, 1024))))
-    return f"sm{sm_count}/seeds{bucket}/stage{sbucket}/out{layout.n_pairs * layout.n_b}x{n_dirs}"
+    return f"lib{N.lib_digest()}/sm{sm_count}/seeds{bucket}/stage{sbucket}/out{layout.n_pairs * layout.n_b}x{n_dirs}"
 
 
 def _time(jobs, cfg, layout, dirs, lc, device, reps=2) -> float:
