@@ -536,9 +536,11 @@ def _make_population(rho_um3: float, side: float, cfg: SimConfig, rng: np.random
 
 
 def default_grid_params(rho_per_uL: float, alpha_max: float, L: float,
-                        voxel_per_spacing: float = 0.5, cap_per_spacing: float = 0.125,
+                        voxel_per_spacing: float = 0.5, cap_per_spacing: float = 0.0,
                         max_voxels_per_axis: int = 96) -> Tuple[int, float, float]:
-    """(G, h, cap): voxel edge and Tier-1 cap as fractions of the seed spacing."""
+    """(G, h, cap): voxel edge and the extra candidate-list radius as fractions of
+    the seed spacing (the lists always hold every seed that can be nearest or
+    bind; cap > 0 widens them by that distance)."""
     spacing = _rho_um3(rho_per_uL) ** (-1.0 / 3.0)
     G = int(min(max_voxels_per_axis, max(1, int(np.ceil(L / (voxel_per_spacing * spacing))))))
     h = L / G
@@ -579,7 +581,7 @@ def _tile_periodic(seeds: np.ndarray, annulus: np.ndarray, L: float, margin: flo
 
 def create_ensemble(rho: float, V: float, cfg: Optional[SimConfig] = None, seed: Optional[int] = None,
                     verbose: bool = False, verify_vi: bool = True, *,
-                    voxel_per_spacing: float = 0.5, cap_per_spacing: float = 0.125,
+                    voxel_per_spacing: float = 0.5, cap_per_spacing: float = 0.0,
                     measure_vi: bool = True) -> Ensemble:
     """Build one ensemble for the requested (rho [cells/uL], V [pL]) (madi/ensemble.py:649-757).
 
@@ -708,7 +710,7 @@ def create_dummy_ensemble(cfg: SimConfig) -> Ensemble:
 def ensemble_from_arrays(seeds: np.ndarray, annulus: np.ndarray, L: float, *, source_lo: float,
                          source_hi: float, mean_AV: float = 0.0, rho_per_uL: Optional[float] = None,
                          boundary_mode: str = "si_fatal_escape", n_cells: Optional[int] = None,
-                         voxel_per_spacing: float = 0.5, cap_per_spacing: float = 0.125,
+                         voxel_per_spacing: float = 0.5, cap_per_spacing: float = 0.0,
                          classifier: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None) -> Ensemble:
     """Wrap externally supplied geometry (e.g. a stored golden case) as an Ensemble.
 

@@ -83,7 +83,7 @@ typedef struct madi_geometry {
     int32_t  pad0;
     double   L;                    /* walk box edge                               */
     double   grid_h;               /* voxel edge (G * grid_h >= L)                */
-    double   safe_cap;             /* Tier-1 radius cap the lists were built for  */
+    double   safe_cap;             /* extra list radius (0: nearest + binding only) */
     double   source_lo;            /* walkers start uniform in [lo, hi)^3         */
     double   source_hi;
     double   coord_err;            /* bound on |fp32 seed - fp64 seed| per axis   */
