@@ -313,12 +313,14 @@ MADI_DEV float facet_m(const float4 f, float wx, float wy, float wz) {
     return fmaf(-f.z, wz, fmaf(-f.y, wy, fmaf(-f.x, wx, f.w)));
 }
 
-// Four smallest margins of a full facet pass (facet slots k1..k3), the
-// point w relative to the cell centre cc, and the error bound T at w.
+// Result of a full facet pass: the three facets of smallest margin (slots
+// k1..k3), the smallest margin m1, a lower bound m4 on every other facet's
+// margin, the cell across the most violated facet, the point w relative to the
+// cell centre cc, and the error bound T at w.
 struct FacetTop {
-    float m1, m2, m3, m4;
+    float m1, m4;
     uint32_t k1, k2, k3;
-    int nb1;                    // cell across facet k1
+    int nb1;                    // cell across the facet of margin m1
     float wx, wy, wz, T;
     float4 cc;
 };

@@ -51,14 +51,16 @@ struct TileShared {
 #define FC(k) ts.fc[(k) * blockDim.x + threadIdx.x]
 
 // Per-walker label cache, built at a point q0 of cell c by a full facet pass
-// with margins m1 <= m2 <= m3 <= m4 (facets k1, k2, k3; error bound T0 at q0):
+// (facets k1, k2, k3 of smallest margin, every other facet's margin >= m4 as
+// computed; error bound T0 at q0):
 //   FC(0..2) = facets k1, k2, k3 (n, h);   FC(3) = (w0, R^2);
 //   FC(4) = (c, alpha_c + Tm);   FC(5) = (alpha_c - Tm, Tm, c, cell across k1),
 // Tm = 3 T0.  Every other facet k has exact m_k(q0) >= m4 - T0 and is
 // 1-Lipschitz, so for |w - w0| < R = m4 - alpha_c - 8 T0 it stays above
 // alpha_c + T(q) (T(q) <= Tm there, and the w rounding of both points adds at
 // most T(q) + T0): for q in the Voronoi cell of c (all cached margins > Tm)
-// the label follows from the three cached margins alone, as in facet_label.
+// the label follows from the three cached margins alone, by the facet-plane
+// rule.
 // A point across a cached facet goes to a full pass (the facet list of c does
 // not bound the seeds beyond it), started in the cell across k1 when k1 is
 // the facet crossed.
@@ -122,8 +124,8 @@ MADI_DEV void merge4(uint32_t& a0, uint32_t& a1, uint32_t& a2, uint32_t& a3, uin
 // three smallest keys name the cached facets, whose margins are recomputed
 // exactly (the true smallest margin is among them unless four margins lie
 // within 2^-17 relative of each other, which the widened band covers); the
-// fourth key bounds every other facet from below.  The group decides as
-// facet_label and its first lane writes the walker's label cache.  A walker
+// fourth key bounds every other facet from below.  The group decides by the
+// facet-plane rule and its first lane writes the walker's label cache.  A walker
 // whose point lies across a facet is queued again from the cell beyond the
 // most violated facet (at most three moves).  Called by all 32 lanes; `start`
 // is each walker's first cell.  Returns FACET_IN / FACET_OUT with cell_q
