@@ -1,12 +1,15 @@
 // GB300 walker: one persistent launch walks every (ensemble, p_p) job of a
 // batch.  Work unit = a tile of `tile_walkers` walkers (one per thread) of one
 // job; CTAs pull tiles from a device counter and stage the tile's geometry
-// (seeds + voxel candidate lists) into shared memory when it changes.
+// (seeds, voxel candidate lists, cell facet table) into shared memory when it
+// changes and fits.
 //
 // Per step and walker (fp32 state, madi/walker_gpu.py:574-655 transition):
 //   propose x' = x + N(0, sigma^2 I)  (Philox4x32-10 + Box-Muller),
 //   boundary: fatal escape (SI) or periodic wrap,
-//   classify x' (Tier-1 proven safe sphere, else the voxel-grid rule, else fp64),
+//   classify x' (the walker's label cache of three facet planes, else a
+//   warp-cooperative pass over its cell's facets, else the voxel-grid rule,
+//   else fp64),
 //   m = endpoint membrane count, accept iff U64 < pp^m * 2^64, else revert,
 //   Y'(t) = int_0^t (x - x0) dt by the step trapezoid (fp32 within one storage
 //   interval, fp64 across intervals).

@@ -401,6 +401,7 @@ class DeviceGeometry:
         periodic = ens.boundary_mode == "periodic"
         if ens.is_free_water:
             n_cells, centers, self.facet_stride = 0, np.zeros((0, 4), np.float32), 0
+            self.facet_reach = 0.0
             fpl, fnbr, h_max = np.zeros((0, 4), np.float32), np.zeros(0, np.int32), 0.0
         else:
             n_cells = int(cellid.max()) + 1
@@ -617,7 +618,7 @@ def create_ensemble(rho: float, V: float, cfg: Optional[SimConfig] = None, seed:
         G, h, cap = default_grid_params(rho, float(np.max(annulus)), side, voxel_per_spacing, cap_per_spacing)
         dmax, _ = _nearest_distance_upper_bound(tree, side, max(h / 2.0, 1e-3))
         # A seed farther than dmax + 2 alpha_max + 2 cap from every box point can be
-        # neither nearest, binding, nor within the Tier-1 proof radius.
+        # neither nearest nor binding, nor within the extra list radius cap.
         margin = dmax + 2.0 * float(np.max(annulus)) + 2.0 * cap + np.sqrt(3.0) * h + 1e-6 * side
         cs, ca, cc = _tile_periodic(seeds, annulus, side, margin)
         cert = PopulationCertificate(
