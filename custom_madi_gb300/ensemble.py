@@ -275,6 +275,28 @@ def build_facets(seeds_xyza: np.ndarray, periodic: bool, L: float):
     raise RuntimeError("madi_facets_build: facet count changed between calls")
 
 
+def pack_facets(fbeg: np.ndarray, planes: np.ndarray, nbr: np.ndarray):
+    """(stride, planes [n, stride, 4], nbr [n, stride]) of a facet table at a
+    fixed stride per cell, so the walker loads a cell's slots without first
+    reading where they start.  stride = max count rounded up to 32; unused slots
+    hold (0, 0, 0, 3e38) / -1.  Stride 0 (and empty arrays) when a cell has more
+    than 64 slots: the walker's margin keys carry the slot in 6 bits, and such a
+    geometry (never met with Poisson seeds) stays on the voxel-grid classifier."""
+    cnt = np.diff(np.asarray(fbeg, np.int64))
+    n = len(cnt)
+    stride = int(max(32, -(-int(cnt.max(initial=0)) // 32) * 32))
+    if stride > 64:
+        return 0, np.zeros((0, 32, 4), np.float32), np.zeros((0, 32), np.int32)
+    fpl = np.zeros((n, stride, 4), np.float32)
+    fpl[:, :, 3] = 3.0e38
+    fnb = np.full((n, stride), -1, np.int32)
+    slot = np.arange(int(cnt.sum())) - np.repeat(np.asarray(fbeg[:-1], np.int64), cnt)
+    row = np.repeat(np.arange(n), cnt)
+    fpl[row, slot] = planes
+    fnb[row, slot] = nbr
+    return stride, fpl, fnb
+
+
 # ---------------------------------------------------------------------------
 # Ensemble
 # ---------------------------------------------------------------------------
@@ -410,25 +432,9 @@ class DeviceGeometry:
                 raise RuntimeError("classifier seeds must list the base cells first")
             fbeg, fpl_csr, fnbr_csr, h_max, self.facet_reach = build_facets(base, periodic, float(ens.L))
             centers = base.astype(np.float32)
-            # fixed stride per cell (a multiple of 32): the walker loads a cell's
-            # slots without first reading where they start
-            cnt = np.diff(fbeg.astype(np.int64))
-            stride = int(max(32, -(-int(cnt.max()) // 32) * 32))
-            if stride > 64:
-                # margin keys carry the slot in 6 bits; a cell with more than 64
-                # facets (never met with Poisson seeds) leaves the walker on the
-                # voxel-grid classifier for this geometry
-                n_cells, stride = 0, 32
-                cnt = np.zeros_like(cnt)
-                fpl_csr, fnbr_csr = fpl_csr[:0], fnbr_csr[:0]
-            fpl = np.zeros((n_cells, stride, 4), np.float32)
-            fpl[:, :, 3] = 3.0e38
-            fnbr = np.full((n_cells, stride), -1, np.int32)
-            slot = np.arange(len(fnbr_csr)) - np.repeat(fbeg[:-1].astype(np.int64), cnt)
-            row = np.repeat(np.arange(len(cnt)), cnt)
-            fpl[row, slot] = fpl_csr
-            fnbr[row, slot] = fnbr_csr
-            self.facet_stride = stride
+            self.facet_stride, fpl, fnbr = pack_facets(fbeg, fpl_csr, fnbr_csr)
+            if self.facet_stride == 0:
+                n_cells, self.facet_stride = 0, 32
         self.n_cells = n_cells
         self.facets_mean = float(np.count_nonzero(fnbr >= 0)) / max(n_cells, 1)
         # |m - m_exact| <= 2 e + 2^-21 (h + |w|_1 + L) for fp32 facet margins, taken twice

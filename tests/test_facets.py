@@ -95,3 +95,26 @@ def test_coincident_seeds_are_rejected():
     pts = np.array([[1.0, 1.0, 1.0, 0.1], [1.0, 1.0, 1.0, 0.1], [3.0, 2.0, 1.0, 0.1], [2.0, 4.0, 3.0, 0.1]])
     with pytest.raises(Exception):
         build_facets(pts, True, 5.0)
+
+
+def test_fixed_stride_packing_keeps_every_facet_in_its_cell_block():
+    from custom_madi_gb300.ensemble import pack_facets
+    rng = np.random.default_rng(11)
+    pts = rng.uniform(0.0, 9.0, (70, 3))
+    beg, pl, nbr, _, _ = build_facets(np.c_[pts, np.full(70, 0.2)], True, 9.0)
+    stride, fpl, fnb = pack_facets(beg, pl, nbr)
+    assert stride % 32 == 0 and stride >= int(np.diff(beg.astype(np.int64)).max())
+    assert fpl.shape == (70, stride, 4) and fnb.shape == (70, stride)
+    for c in range(70):
+        k = int(beg[c + 1] - beg[c])
+        np.testing.assert_array_equal(fpl[c, :k], pl[beg[c]:beg[c + 1]])
+        np.testing.assert_array_equal(fnb[c, :k], nbr[beg[c]:beg[c + 1]])
+        assert np.all(fpl[c, k:, 3] == np.float32(3.0e38)) and np.all(fpl[c, k:, :3] == 0.0)
+        assert np.all(fnb[c, k:] == -1)
+
+
+def test_packing_declines_cells_with_more_than_64_slots():
+    from custom_madi_gb300.ensemble import pack_facets
+    beg = np.array([0, 4, 72], np.uint32)
+    stride, fpl, fnb = pack_facets(beg, np.zeros((72, 4), np.float32), np.zeros(72, np.int32))
+    assert stride == 0 and len(fpl) == 0 and len(fnb) == 0
