@@ -785,9 +785,10 @@ __global__ void __launch_bounds__(256) reduce_Y_kernel(const double* __restrict_
 using namespace madi;
 
 extern "C" int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walkers, int32_t n_grid) {
-    (void)tile_walkers;
-    const int64_t acc = 2ll * MADI_MAX_PAIRS * MADI_MAX_B * MADI_MAX_DIRS * 8;
-    return (int64_t)((stage_bytes + 15) & ~15) + acc + 4ll * n_grid + 8ll * n_grid + 16;
+    // the fused layout of fused_smem() at the largest output shape (8 pairs)
+    const int64_t n_out = (int64_t)MADI_MAX_PAIRS * MADI_MAX_B * MADI_MAX_DIRS;
+    return (int64_t)((stage_bytes + 15) & ~15) + 16ll * n_out + 12ll * ((n_grid + 3) & ~3) +
+           (24ll + FC_BYTES_PER_WALKER + 4 * (3 + 3 * MADI_MAX_PAIRS) + 12) * tile_walkers;
 }
 
 static int64_t fused_smem(const madi_walk_desc* d, int np) {

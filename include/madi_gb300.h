@@ -219,7 +219,9 @@ madi_status madi_walk(const madi_walk_desc* desc, void* stream);
  * 2^31 - 1 are rejected (MADI_ERR_CAPACITY).  Calls no cudaMalloc or cudaFree. */
 madi_status madi_walk_noalloc(const madi_walk_desc* desc, void* stream);
 
-/* Shared-memory bytes the fp32 walker needs for a geometry of stage_bytes. */
+/* Upper bound of the dynamic shared memory of one fp32 walker CTA: a staged
+ * geometry of stage_bytes, tile_walkers threads, n_grid storage points, at the
+ * largest output layout (MADI_MAX_PAIRS x MADI_MAX_B x MADI_MAX_DIRS). */
 int64_t madi_walk_smem_bytes(int32_t stage_bytes, int32_t tile_walkers, int32_t n_grid);
 
 /* Resident CTAs per SM of the fp32 walker for this descriptor's shape

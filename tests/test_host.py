@@ -208,3 +208,13 @@ def test_autotune_python_cache_uses_native_store(tmp_path, monkeypatch):
     assert autotune.store("k1", 256, 0, 1, 0, 5.0e9)
     e = autotune.load("k1")
     assert (e.tile_walkers, e.min_blocks) == (256, 1)
+
+
+def test_walk_smem_bytes_bounds_the_fused_layout():
+    """madi_walk_smem_bytes is an upper bound of the walker's fused shared-memory
+    layout (the same sum walker_gpu.WalkBatch sizes its launches with)."""
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300.walker_gpu import FC_BYTES_PER_WALKER
+    for stage, tw, n_grid, n_out, np_ in ((0, 128, 47, 4 * 5 * 24, 4), (4096, 256, 401, 8 * 32 * 32, 8)):
+        need = stage + 16 * n_out + 12 * ((n_grid + 3) // 4 * 4) + (24 + FC_BYTES_PER_WALKER + 4 * (3 + 3 * np_) + 12) * tw
+        assert N.lib().madi_walk_smem_bytes(stage, tw, n_grid) >= need
