@@ -118,3 +118,22 @@ def test_packing_declines_cells_with_more_than_64_slots():
     beg = np.array([0, 4, 72], np.uint32)
     stride, fpl, fnb = pack_facets(beg, np.zeros((72, 4), np.float32), np.zeros(72, np.int32))
     assert stride == 0 and len(fpl) == 0 and len(fnb) == 0
+
+
+def test_builder_rejects_bad_arguments_and_reports_capacity():
+    import ctypes as C
+    from custom_madi_gb300 import _native as N
+    pts = np.ascontiguousarray(np.c_[np.random.default_rng(2).uniform(0, 5.0, (20, 3)), np.full(20, 0.1)])
+    begin = np.zeros(21, np.uint32)
+    total = C.c_int64(0)
+    lib = N.lib()
+    # one seed, or a periodic box without an edge, is rejected
+    assert lib.madi_facets_build(pts.ctypes.data, 1, 1, 5.0, begin.ctypes.data, None, None, 0, C.byref(total), None) == N.MADI_ERR_INVALID
+    assert lib.madi_facets_build(pts.ctypes.data, 20, 1, 0.0, begin.ctypes.data, None, None, 0, C.byref(total), None) == N.MADI_ERR_INVALID
+    # too small an output: MADI_ERR_CAPACITY with the size needed
+    planes = np.zeros((4, 4), np.float32)
+    nbr = np.zeros(4, np.int32)
+    st = lib.madi_facets_build(pts.ctypes.data, 20, 1, 5.0, begin.ctypes.data, planes.ctypes.data, nbr.ctypes.data, 4,
+                               C.byref(total), None)
+    assert st == N.MADI_ERR_CAPACITY and total.value > 4
+    assert "capacity" in lib.madi_last_error_string().decode()
