@@ -608,6 +608,21 @@ def results_to_reduced(ens: Ensemble, pp: float, cfg: SimConfig, r: dict, n_walk
         n_dirs=n_dirs)
 
 
+def _walk_and_reduce_one_ensemble(ens: Ensemble, pp: float, cfg: SimConfig, j_delta, j_Delta, j_sum, phase_coef,
+                                  walk_seed: int, *, narrow_snapshot_steps=None, narrow_snapshot_index=None,
+                                  narrow_phase_coef=None) -> ReducedResult:
+    """One ensemble at one p_p, reduced over the columns (the reference helper of
+    the same name, madi/walker_gpu.py:989-1063, called by its benchmark scripts).
+    The reference walks in cfg.walker_chunk chunks seeded walk_seed + offset;
+    here all cfg.n_walkers walkers are one job keyed by walk_seed in one launch.
+    Escapes raise the same RuntimeError; narrow-pulse arrays raise ValueError."""
+    _check_narrow(cfg, (narrow_snapshot_steps, narrow_snapshot_index, narrow_phase_coef))
+    pp = _checked_pp(pp)
+    n = int(cfg.n_walkers)
+    r = simulate_jobs([WalkJob(ens, pp, int(walk_seed), n)], cfg, (j_delta, j_Delta, j_sum, phase_coef))[0]
+    return results_to_reduced(ens, pp, cfg, r, n)
+
+
 def _merge_results(results: Sequence[ReducedResult]) -> ReducedResult:
     """Sum in ensemble order; per-ensemble lists are concatenated unsorted (CRN partner order)."""
     if not results:

@@ -272,3 +272,24 @@ def test_per_step_labels_match_oracle_on_periodic_box(n_cells):
     # the facet table decided nearly every step; the voxel-grid rule is the rare fallback
     c = tel["classifier_cache"]
     assert c["tier1"] >= 0.99 * n * steps and c["facet_pass"] > 0
+
+
+def test_walk_and_reduce_one_ensemble_helper():
+    """The reference's private helper (used by its benchmark scripts) walks one
+    ensemble at one p_p and returns the reduced result of the batched walk."""
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.walker_gpu import (WalkJob, _walk_and_reduce_one_ensemble, kio_to_pp, results_to_reduced,
+                                              simulate_jobs)
+    cfg, ens = _periodic_c0(2000)
+    cols = S.build_columns(cfg)
+    pp = kio_to_pp(20.0, ens.mean_AV, cfg)
+    cfg2 = cfg                      # n_walkers = 2000
+    got = _walk_and_reduce_one_ensemble(ens, pp, cfg2, cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef, 77)
+    r = simulate_jobs([WalkJob(ens, pp, 77, 2000)], cfg2, (cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef))[0]
+    want = results_to_reduced(ens, pp, cfg2, r, 2000)
+    assert got.n_walkers == 2000 and got.n_escaped == 0
+    np.testing.assert_array_equal(got.cos_sum, want.cos_sum)
+    np.testing.assert_array_equal(got.occupancy_counts, want.occupancy_counts)
+    with pytest.raises(ValueError):
+        _walk_and_reduce_one_ensemble(ens, pp, cfg2, cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef, 77,
+                                      narrow_snapshot_steps=np.zeros(1))
