@@ -62,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     for name in CPP_SOURCES:
         src, obj = CSRC / name, OBJDIR / (name + ".o")
         if force or _stale(obj, src):
-            jobs.append([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-x", "c++",
+            jobs.append([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-pthread", "-x", "c++",
                          "-c", str(src), "-o", str(obj)])
 
     def run(cmd):
@@ -79,7 +79,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     objs = [OBJDIR / (n + ".o") for n in CU_SOURCES + CPP_SOURCES]
     if force or jobs or not out.exists():
         tmp = out.with_suffix(".so.tmp")
-        run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs)])
+        run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs), "-lpthread"])
         os.replace(tmp, out)
     return out
 

@@ -13,6 +13,7 @@
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 #include "madi_host.h"
 
 namespace madi {
@@ -359,6 +360,86 @@ struct Polytope {
 };
 }  // namespace
 
+namespace {
+// Facet records of a range of cells, in order: per cell its padded record count.
+struct FacetChunk {
+    std::vector<float> planes;      // 4 floats per record
+    std::vector<int32_t> nbr;
+    std::vector<uint32_t> count;
+    double h_max = 0.0, reach = 0.0;
+    int32_t err_cell = -1, err_other = -1;
+};
+
+struct FacetInput {
+    const double* seeds;
+    const std::vector<double>* pts;     // candidates: x, y, z, base id
+    const Bins* B;
+    double spacing, r_max;
+};
+
+void facets_range(const FacetInput& X, int32_t c0, int32_t c1, FacetChunk& out) {
+    const std::vector<double>& pts = *X.pts;
+    std::vector<std::pair<double, int32_t>> cand;
+    std::vector<const Face*> fl;
+    for (int32_t c = c0; c < c1; ++c) {
+        const double* sc = X.seeds + 4 * (size_t)c;
+        const P3 x0{sc[0], sc[1], sc[2]};
+        Polytope P;
+        bool closed = false;
+        for (double r = std::min(3.0 * X.spacing, X.r_max);; r = std::min(2.0 * r, X.r_max)) {
+            cand.clear();
+            const double blo[3] = {x0.x - r, x0.y - r, x0.z - r}, bhi[3] = {x0.x + r, x0.y + r, x0.z + r};
+            for_bins_in_box(*X.B, blo, bhi, [&](int32_t j) {
+                const P3 u = P3{pts[4 * (size_t)j], pts[4 * (size_t)j + 1], pts[4 * (size_t)j + 2]} - x0;
+                const double d = norm(u);
+                if (d <= r && !(d == 0.0 && (int32_t)pts[4 * (size_t)j + 3] == c)) cand.push_back({d, j});
+            });
+            std::sort(cand.begin(), cand.end());
+            P.eps = 1e-9 * r;
+            P.cube(r);
+            bool ended = false;
+            for (const auto& cj : cand) {
+                if (cj.first == 0.0) {
+                    out.err_cell = c;
+                    out.err_other = (int32_t)pts[4 * (size_t)cj.second + 3];
+                    return;
+                }
+                if (0.5 * cj.first > P.radius() + P.eps) { ended = true; break; }
+                const size_t j = (size_t)cj.second;
+                const P3 u = P3{pts[4 * j], pts[4 * j + 1], pts[4 * j + 2]} - x0;
+                const P3 nv = (1.0 / cj.first) * u;
+                const double h = 0.5 * cj.first;
+                if (P.excess(nv, h) < -P.eps) continue;
+                P.clip(nv, h, (int32_t)pts[4 * j + 3]);
+            }
+            if (ended || 2.0 * (P.radius() + P.eps) <= r) { closed = true; break; }
+            if (r >= X.r_max) break;
+        }
+        fl.clear();
+        if (closed) {
+            for (const Face& f : P.faces)
+                if (f.nbr >= 0) fl.push_back(&f);
+            std::sort(fl.begin(), fl.end(), [](const Face* a, const Face* b) { return a->h < b->h; });
+            out.reach = std::max(out.reach, P.radius());
+            for (const Face* f : fl) out.h_max = std::max(out.h_max, f->h);
+        }
+        const int64_t nf = closed ? (int64_t)fl.size() : 0;
+        const int64_t padded = std::max<int64_t>(4, (nf + 3) & ~3ll);
+        for (int64_t k = 0; k < padded; ++k) {
+            if (k < nf) {
+                const Face* f = fl[k];
+                out.planes.insert(out.planes.end(), {(float)f->n.x, (float)f->n.y, (float)f->n.z, (float)f->h});
+                out.nbr.push_back(f->nbr);
+            } else {
+                out.planes.insert(out.planes.end(), {0.0f, 0.0f, 0.0f, closed ? 3.0e38f : -3.0e38f});
+                out.nbr.push_back(-1);
+            }
+        }
+        out.count.push_back((uint32_t)padded);
+    }
+}
+}  // namespace
+
 extern "C" madi_status madi_facets_build(const double* seeds, int32_t n, int32_t periodic, double L,
                                          uint32_t* begin, float* planes, int32_t* nbr, int64_t capacity,
                                          int64_t* total, double* stats) {
@@ -385,77 +466,50 @@ extern "C" madi_status madi_facets_build(const double* seeds, int32_t n, int32_t
     const double ext = periodic ? L : std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-30});
     const double spacing = std::cbrt(ext * ext * ext / n);
     const Bins B = make_bins(pts.data(), np, spacing);
-    // periodic: images within +-1 box cover every candidate up to r = L
-    const double r_max = periodic ? L : 4.0 * ext;
+    // periodic: images within +-1 box cover every candidate up to r = L.  A
+    // finite population's cells close within a few spacings except on its outer
+    // surface; past 12 spacings a cell is left open (the walker's voxel-grid
+    // classifier decides there) instead of scanning the whole population.
+    const FacetInput X{seeds, &pts, &B, spacing, periodic ? L : std::min(4.0 * ext, 12.0 * spacing)};
+    // cells are independent: contiguous ranges on host threads, joined in order
+    const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+    const int T = std::max(1, std::min({hw, 32, (n + 255) / 256}));
+    std::vector<FacetChunk> chunks(T);
+    std::vector<std::thread> workers;
+    for (int t = 1; t < T; ++t)
+        workers.emplace_back(facets_range, std::cref(X), (int32_t)((int64_t)n * t / T),
+                             (int32_t)((int64_t)n * (t + 1) / T), std::ref(chunks[t]));
+    facets_range(X, 0, (int32_t)((int64_t)n / T), chunks[0]);
+    for (std::thread& w : workers) w.join();
+    for (const FacetChunk& ch : chunks)
+        if (ch.err_cell >= 0)
+            return host::fail(MADI_ERR_GEOMETRY, "facets_build: seeds %d and %d coincide", ch.err_cell, ch.err_other);
     int64_t count = 0;
     double h_max = 0.0, reach = 0.0;
-    std::vector<std::pair<double, int32_t>> cand;
-    std::vector<const Face*> fl;
-    for (int32_t c = 0; c < n; ++c) {
-        const P3 x0{seeds[4 * (size_t)c], seeds[4 * (size_t)c + 1], seeds[4 * (size_t)c + 2]};
-        Polytope P;
-        bool closed = false;
-        for (double r = std::min(3.0 * spacing, r_max);; r = std::min(2.0 * r, r_max)) {
-            cand.clear();
-            const double blo[3] = {x0.x - r, x0.y - r, x0.z - r}, bhi[3] = {x0.x + r, x0.y + r, x0.z + r};
-            for_bins_in_box(B, blo, bhi, [&](int32_t j) {
-                const P3 u = P3{pts[4 * (size_t)j], pts[4 * (size_t)j + 1], pts[4 * (size_t)j + 2]} - x0;
-                const double d = norm(u);
-                if (d <= r && !(d == 0.0 && (int32_t)pts[4 * (size_t)j + 3] == c)) cand.push_back({d, j});
-            });
-            std::sort(cand.begin(), cand.end());
-            P.eps = 1e-9 * r;
-            P.cube(r);
-            bool ended = false;
-            for (const auto& cj : cand) {
-                if (cj.first == 0.0)
-                    return host::fail(MADI_ERR_GEOMETRY, "facets_build: seeds %d and %d coincide", c,
-                                      (int)pts[4 * (size_t)cj.second + 3]);
-                if (0.5 * cj.first > P.radius() + P.eps) { ended = true; break; }
-                const size_t j = (size_t)cj.second;
-                const P3 u = P3{pts[4 * j], pts[4 * j + 1], pts[4 * j + 2]} - x0;
-                const P3 nv = (1.0 / cj.first) * u;
-                const double h = 0.5 * cj.first;
-                if (P.excess(nv, h) < -P.eps) continue;
-                P.clip(nv, h, (int32_t)pts[4 * j + 3]);
-            }
-            if (ended || 2.0 * (P.radius() + P.eps) <= r) { closed = true; break; }
-            if (r >= r_max) break;
+    int32_t c = 0;
+    for (const FacetChunk& ch : chunks) {
+        for (uint32_t k : ch.count) {
+            begin[c++] = (uint32_t)count;
+            count += k;
         }
-        fl.clear();
-        if (closed) {
-            for (const Face& f : P.faces)
-                if (f.nbr >= 0) fl.push_back(&f);
-            std::sort(fl.begin(), fl.end(), [](const Face* a, const Face* b) { return a->h < b->h; });
-            reach = std::max(reach, P.radius());
-            for (const Face* f : fl) h_max = std::max(h_max, f->h);
-        }
-        begin[c] = (uint32_t)count;
-        const int64_t nf = closed ? (int64_t)fl.size() : 0;
-        const int64_t padded = std::max<int64_t>(4, (nf + 3) & ~3ll);
-        if (planes && count + padded <= capacity) {
-            for (int64_t k = 0; k < padded; ++k) {
-                float* o = planes + 4 * (size_t)(count + k);
-                if (k < nf) {
-                    const Face* f = fl[k];
-                    o[0] = (float)f->n.x; o[1] = (float)f->n.y; o[2] = (float)f->n.z; o[3] = (float)f->h;
-                    if (nbr) nbr[count + k] = f->nbr;
-                } else {
-                    o[0] = o[1] = o[2] = 0.0f;
-                    o[3] = closed ? 3.0e38f : -3.0e38f;
-                    if (nbr) nbr[count + k] = -1;
-                }
-            }
-        }
-        count += padded;
-        if (count > 0xFFFFFFFFll) return host::fail(MADI_ERR_CAPACITY, "facets_build: more than 2^32 facets");
+        h_max = std::max(h_max, ch.h_max);
+        reach = std::max(reach, ch.reach);
     }
+    if (count > 0xFFFFFFFFll) return host::fail(MADI_ERR_CAPACITY, "facets_build: more than 2^32 facets");
     begin[n] = (uint32_t)count;
     *total = count;
     if (stats) { stats[0] = h_max; stats[1] = reach; }
     if (planes && count > capacity)
         return host::fail(MADI_ERR_CAPACITY, "facets_build: capacity %lld < %lld facets", (long long)capacity,
                           (long long)count);
+    if (planes) {
+        int64_t o = 0;
+        for (const FacetChunk& ch : chunks) {
+            std::copy(ch.planes.begin(), ch.planes.end(), planes + 4 * o);
+            if (nbr) std::copy(ch.nbr.begin(), ch.nbr.end(), nbr + o);
+            o += (int64_t)ch.nbr.size();
+        }
+    }
     return MADI_OK;
 }
 

@@ -313,9 +313,10 @@ madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h,
  * nbr_k (periodic: q - c is the nearest image).  Every Voronoi facet of the
  * cell is listed; planes that only touch the polytope may be listed too.  Each
  * cell's range begin[c] .. begin[c + 1] is padded to a multiple of 4 with
- * (0, 0, 0, 3e38) and nbr -1.  A cell whose polytope cannot be closed by the
- * other seeds (an outer cell of a finite population) gets one padded group
- * with h = -3e38, which sends every step there to the voxel-grid classifier.
+ * (0, 0, 0, 3e38) and nbr -1.  A cell whose polytope the other seeds do not
+ * close within 12 seed spacings (the outer cells of a finite population) gets
+ * one padded group with h = -3e38, which sends every step there to the
+ * voxel-grid classifier.
  * begin: [n + 1]; planes: [capacity][4] (fp32, n_k then h_k); nbr: [capacity].
  * If capacity < *total the call fails with MADI_ERR_CAPACITY and *total holds
  * the size needed.  stats (optional, [2]): the largest h over all facets and
