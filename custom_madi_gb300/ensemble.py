@@ -433,8 +433,12 @@ class DeviceGeometry:
             fbeg, fpl_csr, fnbr_csr, h_max, self.facet_reach = build_facets(base, periodic, float(ens.L))
             centers = base.astype(np.float32)
             self.facet_stride, fpl, fnbr = pack_facets(fbeg, fpl_csr, fnbr_csr)
-            if self.facet_stride == 0:
+            # the stage block's byte offsets are uint32: a table that would not
+            # fit leaves the walker on the voxel-grid classifier
+            head = hi.nbytes + cellid.nbytes + offsets.nbytes + ids.nbytes + centers.nbytes + 64
+            if self.facet_stride == 0 or head + fpl.nbytes + fnbr.nbytes >= 2 ** 32:
                 n_cells, self.facet_stride = 0, 32
+                fpl, fnbr = np.zeros((0, 32, 4), np.float32), np.zeros((0, 32), np.int32)
         self.n_cells = n_cells
         self.facets_mean = float(np.count_nonzero(fnbr >= 0)) / max(n_cells, 1)
         # |m - m_exact| <= 2 e + 2^-21 (h + |w|_1 + L) for fp32 facet margins, taken twice
