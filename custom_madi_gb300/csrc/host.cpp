@@ -155,6 +155,71 @@ void for_bins_in_box(const Bins& B, const double lo[3], const double hi[3], F f)
 }
 }  // namespace
 
+namespace {
+// Candidate lists of voxels [v0, v1) (linear index, x fastest), in order.
+struct GridChunk {
+    std::vector<int32_t> ids;
+    std::vector<uint32_t> count;
+};
+
+void grid_range(const double* seeds, const Bins& B, int G, double h, double eps, double amax, double safe_cap,
+                int64_t v0, int64_t v1, GridChunk& out) {
+    const double span = G * h;
+    std::vector<int32_t> list;
+    for (int64_t v = v0; v < v1; ++v) {
+        const int ix = (int)(v % G), iy = (int)((v / G) % G), iz = (int)(v / ((int64_t)G * G));
+        const double vlo[3] = {ix * h - eps, iy * h - eps, iz * h - eps};
+        const double vhi[3] = {(ix + 1) * h + eps, (iy + 1) * h + eps, (iz + 1) * h + eps};
+        const double c[3] = {0.5 * (vlo[0] + vhi[0]), 0.5 * (vlo[1] + vhi[1]), 0.5 * (vlo[2] + vhi[2])};
+        const double half_diag = 0.5 * std::sqrt(3.0) * (h + 2 * eps);
+        // nearest seed to the centre by growing search boxes
+        double best_c = 1e300;
+        for (double r = B.b;; r *= 2.0) {
+            const double lo[3] = {c[0] - r, c[1] - r, c[2] - r}, hi[3] = {c[0] + r, c[1] + r, c[2] + r};
+            for_bins_in_box(B, lo, hi, [&](int32_t j) {
+                const double* q = seeds + 4 * (size_t)j;
+                const double dx = q[0] - c[0], dy = q[1] - c[1], dz = q[2] - c[2];
+                best_c = std::min(best_c, std::sqrt(dx * dx + dy * dy + dz * dz));
+            });
+            if (best_c <= r - B.b || r > 4.0 * (span + B.b * (B.nb[0] + B.nb[1] + B.nb[2]))) break;
+        }
+        // D(V): min over seeds of the farthest-corner distance; only seeds within
+        // best_c + half_diag of the centre can improve on the nearest one.
+        const double r1 = best_c + half_diag;
+        double D = 1e300;
+        {
+            const double lo[3] = {c[0] - r1, c[1] - r1, c[2] - r1}, hi[3] = {c[0] + r1, c[1] + r1, c[2] + r1};
+            for_bins_in_box(B, lo, hi, [&](int32_t j) {
+                const double* q = seeds + 4 * (size_t)j;
+                double acc = 0.0;
+                for (int a = 0; a < 3; ++a) {
+                    const double e = std::max(std::fabs(q[a] - vlo[a]), std::fabs(q[a] - vhi[a]));
+                    acc += e * e;
+                }
+                D = std::min(D, std::sqrt(acc));
+            });
+        }
+        const double R = (D + 2.0 * amax + 2.0 * safe_cap) * (1.0 + 1e-9) + 1e-9;
+        list.clear();
+        {
+            const double lo[3] = {vlo[0] - R, vlo[1] - R, vlo[2] - R}, hi[3] = {vhi[0] + R, vhi[1] + R, vhi[2] + R};
+            for_bins_in_box(B, lo, hi, [&](int32_t j) {
+                const double* q = seeds + 4 * (size_t)j;
+                double acc = 0.0;
+                for (int a = 0; a < 3; ++a) {
+                    const double e = std::max(std::max(vlo[a] - q[a], q[a] - vhi[a]), 0.0);
+                    acc += e * e;
+                }
+                if (acc <= R * R) list.push_back(j);
+            });
+        }
+        std::sort(list.begin(), list.end());
+        out.ids.insert(out.ids.end(), list.begin(), list.end());
+        out.count.push_back((uint32_t)list.size());
+    }
+}
+}  // namespace
+
 extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h, double eps,
                                        double safe_cap, uint32_t* offsets, void* ids, int32_t ids_u32,
                                        int64_t capacity, int64_t* total) {
@@ -167,71 +232,37 @@ extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G
     const double span = G * h;
     const double spacing = std::cbrt(std::max(span * span * span, 1e-30) / std::max(n, 1));
     const Bins B = make_bins(seeds, n, std::max(h, 0.5 * spacing));
-    std::vector<int32_t> list;
+    // voxels are independent: contiguous ranges on host threads, joined in order
+    const int64_t nv = (int64_t)G * G * G;
+    const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)hw, 32, (nv + 511) / 512}));
+    std::vector<GridChunk> chunks(T);
+    std::vector<std::thread> workers;
+    for (int t = 1; t < T; ++t)
+        workers.emplace_back(grid_range, seeds, std::cref(B), G, h, eps, amax, safe_cap, nv * t / T,
+                             nv * (t + 1) / T, std::ref(chunks[t]));
+    grid_range(seeds, B, G, h, eps, amax, safe_cap, 0, nv / T, chunks[0]);
+    for (std::thread& w : workers) w.join();
     int64_t count = 0;
     if (offsets) offsets[0] = 0;
-    for (int iz = 0; iz < G; ++iz)
-        for (int iy = 0; iy < G; ++iy)
-            for (int ix = 0; ix < G; ++ix) {
-                const double vlo[3] = {ix * h - eps, iy * h - eps, iz * h - eps};
-                const double vhi[3] = {(ix + 1) * h + eps, (iy + 1) * h + eps, (iz + 1) * h + eps};
-                const double c[3] = {0.5 * (vlo[0] + vhi[0]), 0.5 * (vlo[1] + vhi[1]), 0.5 * (vlo[2] + vhi[2])};
-                const double half_diag = 0.5 * std::sqrt(3.0) * (h + 2 * eps);
-                // nearest seed to the centre by growing search boxes
-                double best_c = 1e300;
-                for (double r = B.b;; r *= 2.0) {
-                    const double lo[3] = {c[0] - r, c[1] - r, c[2] - r}, hi[3] = {c[0] + r, c[1] + r, c[2] + r};
-                    for_bins_in_box(B, lo, hi, [&](int32_t j) {
-                        const double* q = seeds + 4 * (size_t)j;
-                        const double dx = q[0] - c[0], dy = q[1] - c[1], dz = q[2] - c[2];
-                        best_c = std::min(best_c, std::sqrt(dx * dx + dy * dy + dz * dz));
-                    });
-                    if (best_c <= r - B.b || r > 4.0 * (span + B.b * (B.nb[0] + B.nb[1] + B.nb[2]))) break;
-                }
-                // D(V): min over seeds of the farthest-corner distance; only seeds within
-                // best_c + half_diag of the centre can improve on the nearest one.
-                const double r1 = best_c + half_diag;
-                double D = 1e300;
-                {
-                    const double lo[3] = {c[0] - r1, c[1] - r1, c[2] - r1}, hi[3] = {c[0] + r1, c[1] + r1, c[2] + r1};
-                    for_bins_in_box(B, lo, hi, [&](int32_t j) {
-                        const double* q = seeds + 4 * (size_t)j;
-                        double acc = 0.0;
-                        for (int a = 0; a < 3; ++a) {
-                            const double e = std::max(std::fabs(q[a] - vlo[a]), std::fabs(q[a] - vhi[a]));
-                            acc += e * e;
-                        }
-                        D = std::min(D, std::sqrt(acc));
-                    });
-                }
-                const double R = (D + 2.0 * amax + 2.0 * safe_cap) * (1.0 + 1e-9) + 1e-9;
-                list.clear();
-                {
-                    const double lo[3] = {vlo[0] - R, vlo[1] - R, vlo[2] - R}, hi[3] = {vhi[0] + R, vhi[1] + R, vhi[2] + R};
-                    for_bins_in_box(B, lo, hi, [&](int32_t j) {
-                        const double* q = seeds + 4 * (size_t)j;
-                        double acc = 0.0;
-                        for (int a = 0; a < 3; ++a) {
-                            const double e = std::max(std::max(vlo[a] - q[a], q[a] - vhi[a]), 0.0);
-                            acc += e * e;
-                        }
-                        if (acc <= R * R) list.push_back(j);
-                    });
-                }
-                std::sort(list.begin(), list.end());
-                if (ids && count + (int64_t)list.size() <= capacity) {
-                    for (size_t t = 0; t < list.size(); ++t) {
-                        if (ids_u32) static_cast<uint32_t*>(ids)[count + t] = (uint32_t)list[t];
-                        else static_cast<uint16_t*>(ids)[count + t] = (uint16_t)list[t];
-                    }
-                }
-                count += (int64_t)list.size();
-                if (offsets) offsets[((size_t)iz * G + iy) * G + ix + 1] = (uint32_t)count;
-            }
+    int64_t v = 0;
+    for (const GridChunk& ch : chunks)
+        for (uint32_t k : ch.count) {
+            count += k;
+            if (offsets && count <= 0xFFFFFFFFll) offsets[++v] = (uint32_t)count;
+        }
     *total = count;
     if (count > 0xFFFFFFFFll) return host::fail(MADI_ERR_CAPACITY, "grid_build: more than 2^32 candidate ids");
     if (ids && count > capacity) return host::fail(MADI_ERR_CAPACITY, "grid_build: capacity %lld < %lld ids",
                                                    (long long)capacity, (long long)count);
+    if (ids) {
+        int64_t o = 0;
+        for (const GridChunk& ch : chunks) {
+            if (ids_u32) std::copy(ch.ids.begin(), ch.ids.end(), static_cast<uint32_t*>(ids) + o);
+            else std::copy(ch.ids.begin(), ch.ids.end(), static_cast<uint16_t*>(ids) + o);
+            o += (int64_t)ch.ids.size();
+        }
+    }
     return MADI_OK;
 }
 

@@ -243,13 +243,17 @@ def build_voxel_grid(seeds_xyza: np.ndarray, G: int, h: float, eps: float, cap: 
     u32 = 1 if n > 65535 else 0
     total = C.c_int64(0)
     offsets = np.zeros(G ** 3 + 1, dtype=np.uint32)
-    st = N.lib().madi_grid_build(s.ctypes.data, n, G, h, eps, cap, None, None, u32, 0, C.byref(total))
-    N.check(st, "madi_grid_build (count)")
-    ids = np.zeros(max(int(total.value), 1), dtype=np.uint32 if u32 else np.uint16)
-    st = N.lib().madi_grid_build(s.ctypes.data, n, G, h, eps, cap, offsets.ctypes.data, ids.ctypes.data,
-                                 u32, len(ids), C.byref(total))
-    N.check(st, "madi_grid_build")
-    return offsets, ids[: int(total.value)], bool(u32)
+    cap_ids = 40 * G ** 3                       # a guess; one retry with the exact size if short
+    for _ in range(2):
+        ids = np.zeros(max(cap_ids, 1), dtype=np.uint32 if u32 else np.uint16)
+        st = N.lib().madi_grid_build(s.ctypes.data, n, G, h, eps, cap, offsets.ctypes.data, ids.ctypes.data,
+                                     u32, len(ids), C.byref(total))
+        if st == N.MADI_ERR_CAPACITY and total.value > cap_ids:
+            cap_ids = int(total.value)
+            continue
+        N.check(st, "madi_grid_build")
+        return offsets, ids[: int(total.value)], bool(u32)
+    raise RuntimeError("madi_grid_build: candidate count changed between calls")
 
 
 def build_facets(seeds_xyza: np.ndarray, periodic: bool, L: float):
