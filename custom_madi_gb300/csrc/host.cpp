@@ -14,6 +14,7 @@
 #include <sstream>
 #include <string>
 #include <thread>
+#include <new>
 #include "madi_host.h"
 
 namespace madi {
@@ -160,6 +161,7 @@ namespace {
 struct GridChunk {
     std::vector<int32_t> ids;
     std::vector<uint32_t> count;
+    bool oom = false;               // a host allocation failed in this range
 };
 
 void grid_range(const double* seeds, const Bins& B, int G, double h, double eps, double amax, double safe_cap,
@@ -238,11 +240,15 @@ extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G
     const int T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)hw, 32, (nv + 511) / 512}));
     std::vector<GridChunk> chunks(T);
     std::vector<std::thread> workers;
-    for (int t = 1; t < T; ++t)
-        workers.emplace_back(grid_range, seeds, std::cref(B), G, h, eps, amax, safe_cap, nv * t / T,
-                             nv * (t + 1) / T, std::ref(chunks[t]));
-    grid_range(seeds, B, G, h, eps, amax, safe_cap, 0, nv / T, chunks[0]);
+    auto run = [&](int64_t v0, int64_t v1, GridChunk* ch) {
+        try { grid_range(seeds, B, G, h, eps, amax, safe_cap, v0, v1, *ch); }
+        catch (const std::bad_alloc&) { ch->oom = true; }
+    };
+    for (int t = 1; t < T; ++t) workers.emplace_back(run, nv * t / T, nv * (t + 1) / T, &chunks[t]);
+    run(0, nv / T, &chunks[0]);
     for (std::thread& w : workers) w.join();
+    for (const GridChunk& ch : chunks)
+        if (ch.oom) return host::fail(MADI_ERR_CAPACITY, "grid_build: out of host memory");
     int64_t count = 0;
     if (offsets) offsets[0] = 0;
     int64_t v = 0;
@@ -399,6 +405,7 @@ struct FacetChunk {
     std::vector<uint32_t> count;
     double h_max = 0.0, reach = 0.0;
     int32_t err_cell = -1, err_other = -1;
+    bool oom = false;               // a host allocation failed in this range
 };
 
 struct FacetInput {
@@ -507,14 +514,18 @@ extern "C" madi_status madi_facets_build(const double* seeds, int32_t n, int32_t
     const int T = std::max(1, std::min({hw, 32, (n + 255) / 256}));
     std::vector<FacetChunk> chunks(T);
     std::vector<std::thread> workers;
+    auto run = [&X](int32_t c0, int32_t c1, FacetChunk* ch) {
+        try { facets_range(X, c0, c1, *ch); } catch (const std::bad_alloc&) { ch->oom = true; }
+    };
     for (int t = 1; t < T; ++t)
-        workers.emplace_back(facets_range, std::cref(X), (int32_t)((int64_t)n * t / T),
-                             (int32_t)((int64_t)n * (t + 1) / T), std::ref(chunks[t]));
-    facets_range(X, 0, (int32_t)((int64_t)n / T), chunks[0]);
+        workers.emplace_back(run, (int32_t)((int64_t)n * t / T), (int32_t)((int64_t)n * (t + 1) / T), &chunks[t]);
+    run(0, (int32_t)((int64_t)n / T), &chunks[0]);
     for (std::thread& w : workers) w.join();
-    for (const FacetChunk& ch : chunks)
+    for (const FacetChunk& ch : chunks) {
+        if (ch.oom) return host::fail(MADI_ERR_CAPACITY, "facets_build: out of host memory");
         if (ch.err_cell >= 0)
             return host::fail(MADI_ERR_GEOMETRY, "facets_build: seeds %d and %d coincide", ch.err_cell, ch.err_other);
+    }
     int64_t count = 0;
     double h_max = 0.0, reach = 0.0;
     int32_t c = 0;
