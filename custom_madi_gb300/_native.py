@@ -20,6 +20,7 @@ MADI_ERR_CAPACITY = 3
 MADI_ERR_TIMEOUT = 4
 MADI_ERR_UNSUPPORTED = 5
 MADI_ERR_GEOMETRY = 6
+MADI_ERR_HOST_MEMORY = 7
 
 MADI_BOUNDARY_FATAL = 0
 MADI_BOUNDARY_PERIODIC = 1

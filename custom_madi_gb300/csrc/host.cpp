@@ -35,6 +35,31 @@ madi_status cuda_fail(cudaError_t e, const char* what) {
     return fail(MADI_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
 }
 }  // namespace host
+
+// Runs job(t) for t in [0, T): t >= 1 on new threads where the system gives
+// them, every other t (always t = 0) on the calling thread; returns when all
+// have ended.  A thread that cannot be created costs time, not correctness:
+// every range is still processed, and the results are joined in order.
+template <class F>
+static void run_parallel(int T, F job) {
+    std::vector<std::thread> workers;
+    std::vector<int> here;
+    try {
+        here.reserve(T);
+        workers.reserve(T);
+    } catch (...) {
+    }
+    here.push_back(0);
+    for (int t = 1; t < T; ++t) {
+        try {
+            workers.emplace_back(job, t);
+        } catch (...) {
+            here.push_back(t);
+        }
+    }
+    for (int t : here) job(t);
+    for (std::thread& w : workers) w.join();
+}
 }  // namespace madi
 
 using namespace madi;
@@ -82,7 +107,7 @@ struct KdBuilder {
 };
 }  // namespace
 
-extern "C" madi_status madi_kdtree_build(const double* seeds_xyz, int32_t n, int32_t* node_seed,
+static madi_status kdtree_build_impl(const double* seeds_xyz, int32_t n, int32_t* node_seed,
                                          int8_t* node_axis, int32_t* node_left, int32_t* node_right,
                                          int32_t* node_parent) {
     host::clear_error();
@@ -222,7 +247,7 @@ void grid_range(const double* seeds, const Bins& B, int G, double h, double eps,
 }
 }  // namespace
 
-extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h, double eps,
+static madi_status grid_build_impl(const double* seeds, int32_t n, int32_t G, double h, double eps,
                                        double safe_cap, uint32_t* offsets, void* ids, int32_t ids_u32,
                                        int64_t capacity, int64_t* total) {
     host::clear_error();
@@ -239,16 +264,12 @@ extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G
     const int hw = std::max(1, (int)std::thread::hardware_concurrency());
     const int T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)hw, 32, (nv + 511) / 512}));
     std::vector<GridChunk> chunks(T);
-    std::vector<std::thread> workers;
-    auto run = [&](int64_t v0, int64_t v1, GridChunk* ch) {
-        try { grid_range(seeds, B, G, h, eps, amax, safe_cap, v0, v1, *ch); }
-        catch (const std::bad_alloc&) { ch->oom = true; }
-    };
-    for (int t = 1; t < T; ++t) workers.emplace_back(run, nv * t / T, nv * (t + 1) / T, &chunks[t]);
-    run(0, nv / T, &chunks[0]);
-    for (std::thread& w : workers) w.join();
+    run_parallel(T, [&](int t) {
+        try { grid_range(seeds, B, G, h, eps, amax, safe_cap, nv * t / T, nv * (t + 1) / T, chunks[t]); }
+        catch (const std::bad_alloc&) { chunks[t].oom = true; }
+    });
     for (const GridChunk& ch : chunks)
-        if (ch.oom) return host::fail(MADI_ERR_CAPACITY, "grid_build: out of host memory");
+        if (ch.oom) return host::fail(MADI_ERR_HOST_MEMORY, "grid_build: out of host memory");
     int64_t count = 0;
     if (offsets) offsets[0] = 0;
     int64_t v = 0;
@@ -478,7 +499,7 @@ void facets_range(const FacetInput& X, int32_t c0, int32_t c1, FacetChunk& out) 
 }
 }  // namespace
 
-extern "C" madi_status madi_facets_build(const double* seeds, int32_t n, int32_t periodic, double L,
+static madi_status facets_build_impl(const double* seeds, int32_t n, int32_t periodic, double L,
                                          uint32_t* begin, float* planes, int32_t* nbr, int64_t capacity,
                                          int64_t* total, double* stats) {
     host::clear_error();
@@ -513,16 +534,12 @@ extern "C" madi_status madi_facets_build(const double* seeds, int32_t n, int32_t
     const int hw = std::max(1, (int)std::thread::hardware_concurrency());
     const int T = std::max(1, std::min({hw, 32, (n + 255) / 256}));
     std::vector<FacetChunk> chunks(T);
-    std::vector<std::thread> workers;
-    auto run = [&X](int32_t c0, int32_t c1, FacetChunk* ch) {
-        try { facets_range(X, c0, c1, *ch); } catch (const std::bad_alloc&) { ch->oom = true; }
-    };
-    for (int t = 1; t < T; ++t)
-        workers.emplace_back(run, (int32_t)((int64_t)n * t / T), (int32_t)((int64_t)n * (t + 1) / T), &chunks[t]);
-    run(0, (int32_t)((int64_t)n / T), &chunks[0]);
-    for (std::thread& w : workers) w.join();
+    run_parallel(T, [&](int t) {
+        try { facets_range(X, (int32_t)((int64_t)n * t / T), (int32_t)((int64_t)n * (t + 1) / T), chunks[t]); }
+        catch (const std::bad_alloc&) { chunks[t].oom = true; }
+    });
     for (const FacetChunk& ch : chunks) {
-        if (ch.oom) return host::fail(MADI_ERR_CAPACITY, "facets_build: out of host memory");
+        if (ch.oom) return host::fail(MADI_ERR_HOST_MEMORY, "facets_build: out of host memory");
         if (ch.err_cell >= 0)
             return host::fail(MADI_ERR_GEOMETRY, "facets_build: seeds %d and %d coincide", ch.err_cell, ch.err_other);
     }
@@ -575,6 +592,49 @@ bool parse_line(const std::string& line, std::string& key, madi_launch_shape& sh
                              sh.walker_steps_per_s);
 }
 }  // namespace
+
+
+// C entry point: no C++ exception crosses the ABI (host allocation failures
+// return MADI_ERR_HOST_MEMORY).
+extern "C" madi_status madi_kdtree_build(const double* seeds_xyz, int32_t n, int32_t* node_seed,
+                                         int8_t* node_axis, int32_t* node_left, int32_t* node_right,
+                                         int32_t* node_parent) {
+    try {
+        return kdtree_build_impl(seeds_xyz, n, node_seed, node_axis, node_left, node_right, node_parent);
+    } catch (const std::bad_alloc&) {
+        return host::fail(MADI_ERR_HOST_MEMORY, "kdtree_build: out of host memory");
+    } catch (...) {
+        return host::fail(MADI_ERR_INVALID, "kdtree_build: unexpected host error");
+    }
+}
+
+// C entry point: no C++ exception crosses the ABI (host allocation failures
+// return MADI_ERR_HOST_MEMORY).
+extern "C" madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h, double eps,
+                                       double safe_cap, uint32_t* offsets, void* ids, int32_t ids_u32,
+                                       int64_t capacity, int64_t* total) {
+    try {
+        return grid_build_impl(seeds, n, G, h, eps, safe_cap, offsets, ids, ids_u32, capacity, total);
+    } catch (const std::bad_alloc&) {
+        return host::fail(MADI_ERR_HOST_MEMORY, "grid_build: out of host memory");
+    } catch (...) {
+        return host::fail(MADI_ERR_INVALID, "grid_build: unexpected host error");
+    }
+}
+
+// C entry point: no C++ exception crosses the ABI (host allocation failures
+// return MADI_ERR_HOST_MEMORY).
+extern "C" madi_status madi_facets_build(const double* seeds, int32_t n, int32_t periodic, double L,
+                                         uint32_t* begin, float* planes, int32_t* nbr, int64_t capacity,
+                                         int64_t* total, double* stats) {
+    try {
+        return facets_build_impl(seeds, n, periodic, L, begin, planes, nbr, capacity, total, stats);
+    } catch (const std::bad_alloc&) {
+        return host::fail(MADI_ERR_HOST_MEMORY, "facets_build: out of host memory");
+    } catch (...) {
+        return host::fail(MADI_ERR_INVALID, "facets_build: unexpected host error");
+    }
+}
 
 extern "C" madi_status madi_autotune_load(const char* path, const char* key, madi_launch_shape* out) {
     host::clear_error();

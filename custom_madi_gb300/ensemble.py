@@ -252,7 +252,8 @@ def build_voxel_grid(seeds_xyza: np.ndarray, G: int, h: float, eps: float, cap: 
             cap_ids = int(total.value)
             continue
         N.check(st, "madi_grid_build")
-        return offsets, ids[: int(total.value)], bool(u32)
+        # a copy, so the oversized guess is freed before the stage block is packed
+        return offsets, ids[: int(total.value)].copy(), bool(u32)
     raise RuntimeError("madi_grid_build: candidate count changed between calls")
 
 
@@ -452,11 +453,13 @@ class DeviceGeometry:
         def pad16(b: bytes) -> bytes:
             return b + b"\0" * ((-len(b)) % 16)
 
+        offs = stage_offsets([a.nbytes for a in (hi, cellid, offsets, ids, centers, fpl, fnbr)])
         parts = [hi.tobytes(), pad16(cellid.tobytes()), pad16(offsets.tobytes()), pad16(ids.tobytes()),
                  pad16(centers.tobytes()), pad16(fpl.tobytes()), pad16(fnbr.tobytes())]
-        offs = np.cumsum([0] + [len(p) for p in parts])
         off_cell, off_go, off_gi = int(offs[1]), int(offs[2]), int(offs[3])
         blob = b"".join(parts)
+        if len(blob) != int(offs[-1]):
+            raise RuntimeError("stage block layout mismatch")
         self.stage = torch.frombuffer(bytearray(blob), dtype=torch.uint8).to(device)
         self.seed_f64 = torch.from_numpy(xyza).to(device)
         if ens.kd_node_seed is None or len(ens.kd_node_seed) != n:
@@ -492,6 +495,23 @@ class DeviceGeometry:
         """Device bytes held by this geometry (stage blob, fp64 seeds, KD arrays)."""
         ts = [self.stage, self.seed_f64, *self.kd]
         return int(sum(t.numel() * t.element_size() for t in ts))
+
+
+def stage_offsets(part_bytes) -> np.ndarray:
+    """Byte offsets of the parts of a geometry's stage block, each part padded
+    to 16 bytes (the first is already a multiple of 16); the last entry is the
+    block's size.  The walker reads these offsets and the size as uint32, so a
+    block of 4 GiB or more is refused here with MADI_ERR_CAPACITY rather than
+    stored wrapped (a ctypes uint32 field keeps only the low 32 bits)."""
+    sizes = [int(b) for b in part_bytes]
+    if any(b < 0 for b in sizes):
+        raise ValueError("stage part sizes must be non-negative")
+    offs = np.cumsum([0] + [b + (-b) % 16 for b in sizes], dtype=np.int64)
+    if int(offs[-1]) >= 2 ** 32:
+        raise N.MadiError(N.MADI_ERR_CAPACITY,
+                          f"geometry stage block of {int(offs[-1])} bytes exceeds the 4 GiB the walker addresses "
+                          "with 32-bit offsets (seeds {}, voxel-grid ids {} B)".format(sizes[0] // 16, sizes[3]))
+    return offs
 
 
 # ---------------------------------------------------------------------------

@@ -34,7 +34,8 @@ typedef enum madi_status {
     MADI_ERR_CAPACITY = 3,     /* an output or scratch capacity is too small                */
     MADI_ERR_TIMEOUT = 4,      /* a bounded device or host wait ran out                     */
     MADI_ERR_UNSUPPORTED = 5,  /* configuration this build does not handle                 */
-    MADI_ERR_GEOMETRY = 6      /* geometry the classifier cannot prove (RuntimeError)       */
+    MADI_ERR_GEOMETRY = 6,     /* geometry the classifier cannot prove (RuntimeError)       */
+    MADI_ERR_HOST_MEMORY = 7   /* a host allocation failed; size outputs are not written    */
 } madi_status;
 
 /* ------------------------------------------------------------------------ */
@@ -298,7 +299,9 @@ madi_status madi_kdtree_build(const double* seeds_xyz, int32_t n, int32_t* node_
 
 /* Candidate lists of a G^3 voxel grid over [0, G*h)^3 (madi_geometry above).
  * seeds: [n][4] x, y, z, alpha.  Two passes: call with ids == NULL to get
- * *total, then with capacity >= *total. */
+ * *total, then with capacity >= *total (MADI_ERR_CAPACITY with *total set
+ * when it is smaller).  MADI_ERR_HOST_MEMORY: the host ran out of memory and
+ * *total is not written. */
 madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h,
                             double eps, double safe_cap, uint32_t* offsets,
                             void* ids, int32_t ids_u32, int64_t capacity, int64_t* total);
@@ -319,8 +322,9 @@ madi_status madi_grid_build(const double* seeds, int32_t n, int32_t G, double h,
  * voxel-grid classifier.
  * begin: [n + 1]; planes: [capacity][4] (fp32, n_k then h_k); nbr: [capacity].
  * If capacity < *total the call fails with MADI_ERR_CAPACITY and *total holds
- * the size needed.  stats (optional, [2]): the largest h over all facets and
- * the largest distance from a seed to a vertex of its closed cell. */
+ * the size needed; MADI_ERR_HOST_MEMORY (host out of memory) leaves *total
+ * unwritten.  stats (optional, [2]): the largest h over all facets and the
+ * largest distance from a seed to a vertex of its closed cell. */
 madi_status madi_facets_build(const double* seeds, int32_t n, int32_t periodic, double L,
                               uint32_t* begin, float* planes, int32_t* nbr,
                               int64_t capacity, int64_t* total, double* stats);

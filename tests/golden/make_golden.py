@@ -1,12 +1,16 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference at REFERENCE_ROOT (default
-/root/reference, read-only).  The reference package imports matplotlib
-unconditionally; a two-file stub is placed on sys.path for the import.  The
-fixtures are small .npz / .json files that the tests read; nothing at test time
-imports the reference.
+The reference checkout is named on the command line (or by the
+MADI_REFERENCE_ROOT environment variable); it is only read.  The reference
+package imports matplotlib unconditionally; a two-file stub is placed on
+sys.path for the import.  The fixtures are small .npz / .json files that the
+tests read; nothing at test time imports the reference.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference PATH [--only base|api]
+
+``base`` writes the classifier, walk, matcher, analytic, population and
+library fixtures; ``api`` the host-API fixtures (random stream, result merge,
+Bayes fit).  Without ``--only`` both are written.
 """
 
 from __future__ import annotations
@@ -21,7 +25,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REFERENCE_ROOT = Path(os.environ.get("MADI_REFERENCE_ROOT", "/root/reference"))
+REFERENCE_ROOT: Path = None  # set by main() from --reference / MADI_REFERENCE_ROOT
 
 
 def _import_reference():
@@ -48,7 +52,26 @@ def _test_reference_table(path: Path, ens_mod) -> Path:
     return path
 
 
-def main() -> int:
+def main(argv=None) -> int:
+    import argparse
+    global REFERENCE_ROOT
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--reference", default=os.environ.get("MADI_REFERENCE_ROOT"),
+                    help="path of the reference checkout (the directory holding the madi package)")
+    ap.add_argument("--only", choices=("base", "api"), default=None)
+    args = ap.parse_args(argv)
+    if not args.reference or not (Path(args.reference) / "madi" / "__init__.py").exists():
+        ap.error("--reference (or MADI_REFERENCE_ROOT) must name a checkout of the reference holding madi/")
+    REFERENCE_ROOT = Path(args.reference)
+    if args.only in (None, "base"):
+        base_fixtures()
+    if args.only in (None, "api"):
+        api_fixtures()
+    print("golden fixtures written to", HERE)
+    return 0
+
+
+def base_fixtures() -> None:
     config, E, W, S, Lb = _import_reference()
     tmp = Path(tempfile.mkdtemp(prefix="madi_golden_"))
     table = _test_reference_table(tmp / "table.npz", E)
@@ -212,8 +235,38 @@ def main() -> int:
                                         metadata={"i": i}))
     Lb._save_library(entries5, str(HERE / "library_v5.npz"), cfg=lcfg, columns=lcols, build_seed=7,
                      grid_metadata={"kind": "fixture"})
-    print("golden fixtures written to", HERE)
-    return 0
+
+
+def api_fixtures() -> None:
+    """Host-API vectors: make_walk_random_stream's draws, _merge_results order."""
+    config, E, W, S, Lb = _import_reference()
+    # ---- 10. make_walk_random_stream (madi/walker_gpu.py:115-127) -------------------
+    scfg = config.SimConfig(L=30.0, n_walkers=5, n_ensembles=1, ts=0.01, T_max_ms=0.04, h_ms=0.01,
+                            small_deltas=[0.01], big_deltas=[0.01], b_values=[0.0])
+    st = W.make_walk_random_stream(scfg, 424242)
+    dummy = E.create_dummy_ensemble(scfg)
+    # ---- 11. _merge_results (madi/walker_gpu.py:1066-1090) --------------------------
+    rng = np.random.default_rng(5)
+    parts = []
+    for e in range(3):
+        parts.append(W.ReducedResult(
+            cos_sum=rng.normal(size=4), sin_sum=rng.normal(size=4), n_walkers=10 + e, n_escaped=0,
+            occupancy_counts=rng.integers(0, 9, 3).astype(np.int64), pp_values=[0.01 * (e + 1)],
+            analytic_kio_eq5_values=[1.5 * (e + 1)], geometry_stats=[{"e": e}],
+            ensemble_cos_means=[rng.normal(size=4)], ensemble_sin_means=[rng.normal(size=4)],
+            classifier_cache_stats=[{"full": e}]))
+    m = W._merge_results(parts)
+    np.savez_compressed(
+        HERE / "api.npz", stream_seed=424242, stream_n_walkers=5, stream_n_steps=scfg.n_steps,
+        stream_L=30.0, stream_source_lo=dummy.source_lo, stream_source_hi=dummy.source_hi,
+        stream_init=st.initial_positions, stream_incr=st.increments, stream_unif=st.acceptance_uniforms,
+        merge_in_cos=np.stack([p.cos_sum for p in parts]), merge_in_sin=np.stack([p.sin_sum for p in parts]),
+        merge_in_occ=np.stack([p.occupancy_counts for p in parts]),
+        merge_in_ens_cos=np.stack([p.ensemble_cos_means[0] for p in parts]),
+        merge_in_ens_sin=np.stack([p.ensemble_sin_means[0] for p in parts]),
+        merge_cos=m.cos_sum, merge_sin=m.sin_sum, merge_n_walkers=m.n_walkers, merge_occ=m.occupancy_counts,
+        merge_pp=np.asarray(m.pp_values), merge_kio=np.asarray(m.analytic_kio_eq5_values),
+        merge_ens_cos=np.asarray(m.ensemble_cos_means), merge_ens_sin=np.asarray(m.ensemble_sin_means))
 
 
 if __name__ == "__main__":

@@ -218,3 +218,19 @@ def test_walk_smem_bytes_bounds_the_fused_layout():
     for stage, tw, n_grid, n_out, np_ in ((0, 128, 47, 4 * 5 * 24, 4), (4096, 256, 401, 8 * 32 * 32, 8)):
         need = stage + 16 * n_out + 12 * ((n_grid + 3) // 4 * 4) + (24 + FC_BYTES_PER_WALKER + 4 * (3 + 3 * np_) + 12) * tw
         assert N.lib().madi_walk_smem_bytes(stage, tw, n_grid) >= need
+
+
+def test_stage_block_refuses_offsets_past_32_bits():
+    """The walker reads stage offsets as uint32: a block of 4 GiB or more (here
+    a voxel grid of 2^32 ids' bytes, given as sizes only) is refused, never
+    stored wrapped."""
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300.ensemble import stage_offsets
+    offs = stage_offsets([16 * 5, 4 * 5, 4 * 9, 2 * 17, 16 * 5, 0, 0])
+    assert offs.tolist() == [0, 80, 112, 160, 208, 288, 288, 288]
+    with pytest.raises(N.MadiError, match="4 GiB") as ei:
+        stage_offsets([16 * 1000, 4 * 1000, 4 * 513, 2 ** 32, 0, 0, 0])
+    assert ei.value.status == N.MADI_ERR_CAPACITY
+    assert int(stage_offsets([16, 16, 16, 2 ** 32 - 16 * 4, 0, 0, 0])[-1]) == 2 ** 32 - 16
+    with pytest.raises(N.MadiError):
+        stage_offsets([16, 16, 16, 2 ** 32 - 16 * 3, 0, 0, 0])      # each part under the limit, the sum at it
