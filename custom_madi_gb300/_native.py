@@ -36,6 +36,7 @@ MADI_MATCH_FIXED_S0 = 0
 MADI_MATCH_FREE_S0 = 1
 MADI_MATCH_FP32 = 0
 MADI_MATCH_BF16 = 1
+MADI_MATCH_FLAG_TEST_STALL = 1
 
 CNT_NAMES = ("walkers", "escaped", "classifier_error", "full", "tier1", "fallback64",
              "cross_accept", "cross_reject", "facet_pass")
@@ -43,7 +44,7 @@ MADI_CNT_N = len(CNT_NAMES)
 
 EXPORTED = (
     "madi_abi_version", "madi_last_error_string", "madi_classify", "madi_walk",
-    "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_scratch_bytes",
+    "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_wait", "madi_match_scratch_bytes",
     "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_walk_blocks_per_sm", "madi_walk_noalloc",
     "madi_walk_batched", "madi_autotune_load", "madi_autotune_store",
     "madi_serve_arena_bytes", "madi_serve_create", "madi_serve_submit", "madi_serve_poll",
@@ -107,7 +108,7 @@ class MadiMatchDesc(C.Structure):
     _fields_ = [
         ("measured", C.c_void_p), ("lib", C.c_void_p), ("n_vox", C.c_int64),
         ("n_lib", C.c_int32), ("n_feat", C.c_int32), ("mode", C.c_int32),
-        ("precision", C.c_int32), ("topk", C.c_int32), ("pad0", C.c_int32),
+        ("precision", C.c_int32), ("topk", C.c_int32), ("flags", C.c_int32),
         ("best_idx", C.c_void_p), ("best_resid", C.c_void_p), ("best_s0", C.c_void_p),
         ("scratch", C.c_void_p), ("scratch_bytes", C.c_int64),
     ]
@@ -163,6 +164,7 @@ def _declare(lib):
     lib.madi_walk_blocks_per_sm.restype = C.c_int32
     lib.madi_reduce_Y.argtypes = [P, C.c_int64, C.c_int32, P, P, P, P, C.c_int32, P, P, P]
     lib.madi_match.argtypes = [C.POINTER(MadiMatchDesc), P]
+    lib.madi_match_wait.argtypes = [C.POINTER(MadiMatchDesc), P]
     lib.madi_match_scratch_bytes.argtypes = [C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     lib.madi_match_scratch_bytes.restype = C.c_int64
     lib.madi_kdtree_build.argtypes = [P, C.c_int32, P, P, P, P, P]
@@ -171,7 +173,7 @@ def _declare(lib):
     lib.madi_facets_build.argtypes = [P, C.c_int32, C.c_int32, C.c_double, P, P, P, C.c_int64,
                                       C.POINTER(C.c_int64), P]
     for name in ("madi_classify", "madi_walk", "madi_walk_noalloc", "madi_walk_batched", "madi_reduce_Y",
-                 "madi_match", "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_autotune_load",
+                 "madi_match", "madi_match_wait", "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_autotune_load",
                  "madi_autotune_store", "madi_serve_create", "madi_serve_submit", "madi_serve_poll",
                  "madi_serve_release", "madi_serve_destroy"):
         getattr(lib, name).restype = C.c_int

@@ -109,6 +109,7 @@ static madi_status launch_fp32(const madi_match_desc* d, float* mu, cudaStream_t
 using namespace madi;
 
 madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s);
+const int* madi_match_bf16_status_word(const madi_match_desc* d);
 int64_t madi_match_bf16_scratch(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t topk);
 void madi_match_column_mean(const float* lib, int32_t n_lib, int32_t n_feat, float* mu, cudaStream_t s);
 
@@ -147,4 +148,26 @@ extern "C" madi_status madi_match(const madi_match_desc* d, void* stream) {
     if (d->n_feat <= 16) return launch_fp32<16>(d, mu, s);
     if (d->n_feat <= 24) return launch_fp32<24>(d, mu, s);
     return launch_fp32<32>(d, mu, s);
+}
+
+extern "C" madi_status madi_match_wait(const madi_match_desc* d, void* stream) {
+    host::clear_error();
+    if (!d) return host::fail(MADI_ERR_INVALID, "match_wait: null descriptor");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return host::cuda_fail(e, "match_wait: stream");
+    if (d->precision != MADI_MATCH_BF16 || d->n_vox == 0) return MADI_OK;
+    if (!d->scratch || d->scratch_bytes < madi_match_bf16_scratch(d->n_vox, d->n_lib, d->n_feat, d->topk))
+        return host::fail(MADI_ERR_INVALID, "match_wait: descriptor has no BF16 scratch");
+    int word = 0;
+    e = cudaMemcpyAsync(&word, madi_match_bf16_status_word(d), sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return host::cuda_fail(e, "match_wait: status word");
+    if (word == 1)
+        return host::fail(MADI_ERR_TIMEOUT, "match bf16: a bounded wait ran out; the rows of the CTAs that gave up "
+                                            "have no result (issued copies and MMAs were drained)");
+    if (word != 0)
+        return host::fail(MADI_ERR_TIMEOUT, "match bf16: a bounded wait ran out and so did the drain of the issued "
+                                            "copies and MMAs");
+    return MADI_OK;
 }

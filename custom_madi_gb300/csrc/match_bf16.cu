@@ -59,6 +59,12 @@ constexpr int WG_COLS = 64;                     // columns per epilogue pass (tw
 constexpr int CAP = 32;                         // per-thread candidate buffer entries
 constexpr uint32_t SUSPEND_NS = 20000;          // mbarrier try_wait suspend hint
 constexpr uint32_t SPIN_LIMIT = 50000;          // bounded waits: <= SPIN_LIMIT * SUSPEND_NS ~ 1 s
+constexpr uint32_t DRAIN_LIMIT = 4 * SPIN_LIMIT; // waits for issued copies / MMAs after an error
+constexpr uint32_t STALL_POLLS = 64;            // the test-only stalled wait (MADI_MATCH_FLAG_TEST_STALL)
+// Status word in the scratch, read by madi_match_wait: 0 ok, 1 a bounded wait
+// ran out (every issued copy and MMA then drained), 2 the drain ran out too.
+constexpr int ERR_TIMEOUT = 1;
+constexpr int ERR_DRAIN = 2;
 
 enum { MODE_FOLD = 0, MODE_AUX = 1, MODE_FREE = 2 };
 
@@ -102,20 +108,20 @@ MADI_DEV void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(bar)) : "memory");
 }
 
-// Bounded parity wait; returns false after SPIN_LIMIT polls.
-MADI_DEV bool mbar_wait(uint64_t* bar, uint32_t parity);
+// Bounded parity wait; returns false after `limit` polls.
+MADI_DEV bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = SPIN_LIMIT);
 
 // Warp-wide bounded wait polled by lane 0 only (the other lanes would only add
 // shared-memory traffic); the result is the same on every lane.
-MADI_DEV bool mbar_wait_warp(uint64_t* bar, uint32_t parity, int lane) {
+MADI_DEV bool mbar_wait_warp(uint64_t* bar, uint32_t parity, int lane, uint32_t limit = SPIN_LIMIT) {
     bool ok = false;
-    if (lane == 0) ok = mbar_wait(bar, parity);
+    if (lane == 0) ok = mbar_wait(bar, parity, limit);
     return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
 }
 
-MADI_DEV bool mbar_wait(uint64_t* bar, uint32_t parity) {
+MADI_DEV bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
     const uint32_t a = smem_u32(bar);
-    for (uint32_t i = 0; i < SPIN_LIMIT; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
                      : "=r"(done) : "r"(a), "r"(parity), "r"(SUSPEND_NS) : "memory");
@@ -627,6 +633,7 @@ struct Plan {
     float* best_resid;
     float* best_s0;
     int* err;
+    int test_stall;                     // tests only: one epilogue wait that nothing completes
 };
 
 struct Smem {
@@ -644,6 +651,8 @@ struct Smem {
     uint64_t afull;
     uint64_t lfull;
     uint64_t drain;
+    uint64_t never;                     // no thread ever arrives (the test-only stalled wait)
+    int64_t n_loaded, n_issued;         // producer: steps whose copies / MMAs were issued
     uint32_t tmem_base;
     int err;
 };
@@ -721,7 +730,8 @@ MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int
     };
     const int64_t n_steps = n_pad / PAIR;
     for (; gl < total && gl < LOAD_AHEAD; ++gl) load(gl);
-    for (int64_t g = 0; g < total && ok; ++g) {
+    int64_t g = 0;                                   // steps whose MMAs were issued
+    for (; g < total && ok; ++g) {
         const int st = (int)(g % STAGES), acc = (int)(g % ACCS);
         if (g >= ACCS && !mbar_wait_warp(&S.acce[acc], (uint32_t)((g / ACCS - 1) & 1), lane)) { ok = false; break; }
         if (gl < total && gl <= g + LOAD_AHEAD) load(gl++);
@@ -743,16 +753,34 @@ MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int
         }
         __syncwarp();
     }
-    if (!ok && lane == 0) {
-        S.err = 1;
-        // let issued copies and MMAs land before TMEM / shared memory go away
-        for (int st = 0; st < STAGES; ++st) {
-            const int64_t last = gl - 1 - ((gl - 1 - st) % STAGES + STAGES) % STAGES;   // last load into st
-            if (last >= 0) mbar_wait(&S.full[st], (uint32_t)((last / STAGES) & 1));
-        }
-        mma_commit(&S.drain);      // arrives once every earlier MMA is done
-        mbar_wait(&S.drain, 0);
+    if (lane == 0) {
+        S.n_loaded = gl;
+        S.n_issued = g;
+        if (!ok) S.err = ERR_TIMEOUT;
     }
+}
+
+// After an error (the epilogue may have left before consuming every step):
+// wait, bounded, for every copy and MMA the producer issued, so that nothing
+// lands in shared memory or TMEM once they are released.  The last load into
+// each stage completes its `full` phase; the last step on each accumulator
+// completes its `accf` phase (the step's aux copies and its MMA commit); a
+// final commit on `drain` covers every earlier MMA.  Each of these is the
+// latest phase of its barrier, so its parity is unambiguous.  Returns false if
+// a wait ran out.
+MADI_DEV bool drain_issued(Smem& S) {
+    const int64_t gl = S.n_loaded, gi = S.n_issued;
+    bool ok = true;
+    for (int st = 0; st < STAGES; ++st) {
+        const int64_t last = gl - 1 - ((gl - 1 - st) % STAGES + STAGES) % STAGES;   // last load into st
+        if (last >= 0) ok = mbar_wait(&S.full[st], (uint32_t)((last / STAGES) & 1), DRAIN_LIMIT) && ok;
+    }
+    for (int a = 0; a < ACCS; ++a) {
+        const int64_t last = gi - 1 - ((gi - 1 - a) % ACCS + ACCS) % ACCS;          // last step on a
+        if (last >= 0) ok = mbar_wait(&S.accf[a], (uint32_t)((last / ACCS) & 1), DRAIN_LIMIT) && ok;
+    }
+    mma_commit(&S.drain);      // arrives once every earlier MMA is done
+    return mbar_wait(&S.drain, 0, DRAIN_LIMIT) && ok;
 }
 
 // fp32 rescore of this thread's k candidates (staged in its buffer, as scan
@@ -831,6 +859,9 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
         mbar_init(&S.afull, 4);
         mbar_init(&S.lfull, 4);
         mbar_init(&S.drain, 1);
+        mbar_init(&S.never, 1);
+        S.n_loaded = 0;
+        S.n_issued = 0;
         S.err = 0;
     }
     if (tid < EPI_THREADS) S.thr_pub[tid / TILE_M][tid % TILE_M] = make_uint2(0xFFFFFFFFu, 0u);
@@ -863,6 +894,10 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
         int64_t g = 0;
         bool ok = true;
         if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, P, blockIdx.x, r, lane);
+        if (P.test_stall && my_vt > 0 && !mbar_wait_warp(&S.never, 0, lane, STALL_POLLS)) {
+            S.err = ERR_TIMEOUT;    // tests only: the wait runs out like any other would
+            ok = false;
+        }
         for (int64_t lv = 0; lv < my_vt && ok; ++lv) {
             const int64_t vt = blockIdx.x + lv * gridDim.x;
             float ks[K];
@@ -882,7 +917,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                 const int acc = (int)(g % ACCS);
                 const bool got = mbar_wait_warp(&S.accf[acc], (uint32_t)((g / ACCS) & 1), lane) &&
                                  !__any_sync(0xffffffffu, err_flag_read(S) != 0);   // warp-uniform
-                if (!got) { S.err = 1; ok = false; break; }
+                if (!got) { S.err = ERR_TIMEOUT; ok = false; break; }
                 fence_after();
                 const int lt = lt_next;
                 if (t + 1 < n_steps) lt_next = my_tile(t + 1);   // prefetch the next step
@@ -1019,7 +1054,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.lfull);
             } else {
-                if (!mbar_wait_warp(&S.lfull, (uint32_t)(lv & 1), lane)) { S.err = 1; ok = false; break; }
+                if (!mbar_wait_warp(&S.lfull, (uint32_t)(lv & 1), lane)) { S.err = ERR_TIMEOUT; ok = false; break; }
                 const float4 o = S.res1[lv & 1][r];
                 const int j1 = __float_as_int(o.y);
                 if (o.x < best || (o.x == best && j1 < bj)) { best = o.x; bj = j1; bs0 = o.z; }
@@ -1031,14 +1066,20 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
             }
         }
     }
-    // ---- teardown: the producer has drained its copies and MMAs on error ----
+    // ---- teardown: after an error, drain what the producer issued first ----
     fence_before();
     __syncthreads();
     fence_after();
+    if (S.err) {
+        if (warp == EPI_WARPS && lane == 0 && !drain_issued(S)) S.err = ERR_DRAIN;
+        fence_before();
+        __syncthreads();
+        fence_after();
+    }
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TMEM_COLS) : "memory");
     }
-    if (tid == 0 && S.err) atomicExch(P.err, 1);
+    if (tid == 0 && S.err) atomicMax(P.err, S.err);
 }
 
 }  // namespace bf16m
@@ -1095,6 +1136,11 @@ unsigned blocks_for(int64_t n, int per) { return (unsigned)((n + per - 1) / per)
 int64_t madi_match_bf16_scratch(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t topk) {
     (void)n_feat; (void)topk;
     return layout(n_vox, n_lib).total;
+}
+
+// Device address of the status word madi_match_bf16 left in the scratch.
+const int* madi_match_bf16_status_word(const madi_match_desc* d) {
+    return reinterpret_cast<const int*>(static_cast<const unsigned char*>(d->scratch) + layout(d->n_vox, d->n_lib).err);
 }
 
 // Library column means (fp64 sums), shared with the fp32 fixed-S0 scan.
@@ -1193,6 +1239,7 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     P.best_resid = d->best_resid;
     P.best_s0 = d->best_s0;
     P.err = err;
+    P.test_stall = (d->flags & MADI_MATCH_FLAG_TEST_STALL) ? 1 : 0;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

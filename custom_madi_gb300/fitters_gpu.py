@@ -31,9 +31,35 @@ def _as_dev(x):
     return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).cuda()
 
 
+class MatchOutput(tuple):
+    """(best_idx, best_resid, best_s0) device tensors of one madi_match call.
+
+    ``check()`` waits for the call and raises ``MadiError`` (a RuntimeError,
+    status MADI_ERR_TIMEOUT) if a bounded wait of the tensor-core scan ran out;
+    the rows it could not finish keep -1 in best_idx.  The inputs and scratch
+    stay referenced until then.
+    """
+
+    def __new__(cls, idx, res, s0, desc, stream, keep):
+        out = super().__new__(cls, (idx, res, s0))
+        out._desc, out._stream, out._keep = desc, stream, keep
+        return out
+
+    def check(self) -> "MatchOutput":
+        st = N.lib().madi_match_wait(C.byref(self._desc), self._stream.cuda_stream)
+        N.check(st, "madi_match")
+        return self
+
+
 def match_device(measured, lib_mat, *, free_s0: bool = False, precision: str = "fp32", topk: int = DEFAULT_TOPK,
-                 scratch=None, stream=None):
-    """Run madi_match on device tensors; returns (best_idx, best_resid, best_s0) device tensors."""
+                 scratch=None, stream=None, check: bool = True, flags: int = 0) -> MatchOutput:
+    """Run madi_match on device tensors; returns (best_idx, best_resid, best_s0) device tensors.
+
+    ``check=True`` waits for the result and raises if the scan could not
+    finish (see ``MatchOutput.check``); ``check=False`` returns as soon as the
+    work is enqueued on ``stream`` and the caller calls ``.check()`` later.
+    ``flags`` is for tests (MADI_MATCH_FLAG_TEST_STALL).
+    """
     if not HAS_CUDA:
         raise RuntimeError("CUDA is unavailable: the library match runs on a CUDA device only")
     M = _as_dev(measured)
@@ -48,12 +74,12 @@ def match_device(measured, lib_mat, *, free_s0: bool = False, precision: str = "
     res = torch.empty(n_vox, dtype=torch.float32, device=M.device)
     s0 = torch.empty(n_vox, dtype=torch.float32, device=M.device) if free_s0 else None
     need = int(N.lib().madi_match_scratch_bytes(n_vox, Lm.shape[0], F, prec, int(topk)))
-    if need > 0 and (scratch is None or scratch.numel() < need):
+    if need > 0 and (scratch is None or scratch.numel() < need + 256):
         scratch = torch.empty(need + 256, dtype=torch.uint8, device=M.device)
     d = N.MadiMatchDesc()
     d.measured, d.lib, d.n_vox, d.n_lib, d.n_feat = N.ptr(M), N.ptr(Lm), n_vox, Lm.shape[0], F
     d.mode = N.MADI_MATCH_FREE_S0 if free_s0 else N.MADI_MATCH_FIXED_S0
-    d.precision, d.topk = prec, int(topk)
+    d.precision, d.topk, d.flags = prec, int(topk), int(flags)
     d.best_idx, d.best_resid, d.best_s0 = N.ptr(idx), N.ptr(res), N.ptr(s0)
     if need > 0:
         base = N.ptr(scratch)
@@ -64,7 +90,8 @@ def match_device(measured, lib_mat, *, free_s0: bool = False, precision: str = "
     s = stream if stream is not None else torch.cuda.current_stream(M.device)
     st = N.lib().madi_match(C.byref(d), s.cuda_stream)
     N.check(st, "madi_match")
-    return idx, res, s0
+    out = MatchOutput(idx, res, s0, d, s, (M, Lm, scratch))
+    return out.check() if check else out
 
 
 def _indices(idx) -> np.ndarray:

@@ -270,7 +270,7 @@ class Server:
                     from .fitters_gpu import match_device
                     with torch.cuda.stream(self.fit_stream):
                         out = match_device(req.voxels, self.library, free_s0=req.free_s0, precision=req.precision,
-                                           topk=req.topk, stream=self.fit_stream)
+                                           topk=req.topk, stream=self.fit_stream, check=False)
                         ev = torch.cuda.Event()
                         ev.record(self.fit_stream)
                     fits.append((ev, rid, out))
@@ -304,6 +304,7 @@ class Server:
                 progressed = True
             while fits and fits[0][0].query():
                 _ev, rid, out = fits.popleft()
+                out.check()               # the scan finished (raises if a bounded wait ran out)
                 idx, res, s0 = out
                 r = recs[rid]
                 r.finish = now()

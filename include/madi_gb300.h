@@ -275,7 +275,7 @@ typedef struct madi_match_desc {
     int32_t mode;                  /* MADI_MATCH_FIXED_S0 / FREE_S0 */
     int32_t precision;             /* MADI_MATCH_FP32 / BF16       */
     int32_t topk;                  /* BF16 candidates rescored     */
-    int32_t pad0;
+    int32_t flags;                 /* 0, or MADI_MATCH_FLAG_*      */
     int32_t* best_idx;             /* [n_vox]                      */
     float*   best_resid;           /* [n_vox]                      */
     float*   best_s0;              /* [n_vox] (free S0) or NULL    */
@@ -283,9 +283,25 @@ typedef struct madi_match_desc {
     int64_t  scratch_bytes;
 } madi_match_desc;
 
+/* Tests only: every CTA of the BF16 scan makes one bounded wait on a barrier
+ * that nothing completes, so the timeout path runs (the CTA drains its issued
+ * copies and MMAs, frees TMEM, leaves its rows at the caller's fill value) and
+ * madi_match_wait reports MADI_ERR_TIMEOUT.  Nothing faults or hangs. */
+#define MADI_MATCH_FLAG_TEST_STALL 1
+
 int64_t madi_match_scratch_bytes(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t precision,
                                  int32_t topk);
 madi_status madi_match(const madi_match_desc* desc, void* stream);
+
+/* Completion status of the last madi_match enqueued with this descriptor on
+ * `stream` (same scratch; no GB300 counterpart: the reference's Numba launch is
+ * synchronous, madi/fitters_gpu.py:414-438).  Synchronizes the stream, then
+ * returns MADI_OK; MADI_ERR_TIMEOUT if a bounded wait of the BF16 scan ran out
+ * (the rows of the CTAs that gave up keep the value the caller left in
+ * best_idx, e.g. -1; every issued copy and MMA was drained before TMEM was
+ * freed, unless the message says the drain ran out too); MADI_ERR_CUDA if the
+ * stream reports an error.  The FP32 scan has no bounded waits. */
+madi_status madi_match_wait(const madi_match_desc* desc, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Host-side geometry builders (native C++; no device work)                 */

@@ -128,3 +128,28 @@ def test_bf16_free_s0_top32_on_rician_voxels():
     d = i16 != i64
     np.testing.assert_allclose(r16.cpu().numpy()[d], r64[d], rtol=1e-4, atol=1e-6)
     np.testing.assert_allclose(s16.cpu().numpy()[~d], s64[~d], rtol=1e-4)
+
+
+def test_bf16_bounded_wait_timeout_is_reported_and_the_device_stays_usable():
+    """A bounded wait of the tensor-core scan that runs out surfaces as
+    MADI_ERR_TIMEOUT from madi_match_wait (and as an exception from
+    match_device), after the CTA drained its issued copies and MMAs and freed
+    TMEM; the next call on the same device and stream gives full results.  The
+    wait is made to run out by the test-only flag (a barrier nothing completes),
+    so no GPU fault is involved."""
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300 import workloads as WL
+    from custom_madi_gb300.fitters_gpu import match_device
+    lib, _ = WL.match_library(n_lib=3000)
+    vox, _ = WL.rician_voxels(lib, n_vox=5000, seed=7)
+    for free in (False, True):
+        out = match_device(vox, lib, precision="bf16", topk=32, free_s0=free, check=False,
+                           flags=N.MADI_MATCH_FLAG_TEST_STALL)
+        with pytest.raises(N.MadiError, match="bounded wait ran out") as ei:
+            out.check()
+        assert ei.value.status == N.MADI_ERR_TIMEOUT
+        assert "were drained" in str(ei.value)                            # drained: the state is sound
+        assert bool((out[0] == -1).all())                                 # no row was written
+        good = match_device(vox, lib, precision="bf16", topk=32, free_s0=free)
+        ref = match_device(vox, lib, precision="fp32", free_s0=free)
+        assert float((good[0] == ref[0]).float().mean()) >= 0.999
