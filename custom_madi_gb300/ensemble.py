@@ -36,7 +36,7 @@ _S7A = (-0.570444, 10.6047, -5.81457, 1.0)   # SI Eq. S7a: v_i(x), x = rho^(1/3)
 
 
 def _rho_um3(rho_per_uL: float) -> float:
-    return float(rho_per_uL) * 1e-9
+    return float(rho_per_uL) / 1.0e9        # the reference's arithmetic (bit-identical v_i, L, alpha*)
 
 
 def _V_um3(V_pL: float) -> float:
@@ -114,9 +114,11 @@ class GeometryStats:
 def alpha_star_from_vi(vi: float, rho_per_uL: float) -> float:
     """alpha* [um] from SI Eq. S7a on its decreasing physical branch.
 
-    v_i(x) is a cubic with v_i(0) = 1 and v_i'(0) < 0; the physical root is the
-    unique one in [0, x_turn], x_turn the first positive stationary point.
-    Solved by bisection to full double precision (monotone bracket).
+    v_i(x) is a cubic in x = rho^(1/3) alpha with v_i(0) = 1 and v_i'(0) < 0;
+    the physical root is the unique real root in [0, x_turn], x_turn the first
+    positive stationary point (a root of v_i').  Both come from numpy's
+    companion-matrix roots, the reference's own arithmetic, so alpha* (and every
+    annulus min(alpha*, kappa d_nn / 2)) is the reference's value bit for bit.
     """
     vi = float(vi)
     rho = _rho_um3(rho_per_uL)
@@ -124,23 +126,13 @@ def alpha_star_from_vi(vi: float, rho_per_uL: float) -> float:
         raise ValueError(f"target v_i must lie in (0, 1), got {vi}")
     if rho <= 0.0:
         raise ValueError("rho must be positive for a cellular geometry")
-    a, b, c, _ = _S7A
-    disc = (2 * b) ** 2 - 4 * (3 * a) * c
-    turns = [(-2 * b + s * np.sqrt(disc)) / (2 * 3 * a) for s in (1.0, -1.0)]
-    x_turn = min(t for t in turns if t > 0.0)
-    lo, hi = 0.0, x_turn
-    if not (_s7a(hi) <= vi <= _s7a(lo)):
-        raise RuntimeError(f"SI Eq. S7a has no physical root for v_i={vi}")
-    for _ in range(200):
-        mid = 0.5 * (lo + hi)
-        if mid == lo or mid == hi:
-            break
-        if _s7a(mid) > vi:
-            lo = mid
-        else:
-            hi = mid
-    x = lo if abs(_s7a(lo) - vi) <= abs(_s7a(hi) - vi) else hi
-    return float(x / rho ** (1.0 / 3.0))
+    a, b, c, d = _S7A
+    x_turn = min(float(t.real) for t in np.roots([3.0 * a, 2.0 * b, c]) if abs(t.imag) < 1e-10 and t.real > 0.0)
+    branch = [float(x.real) for x in np.roots([a, b, c, d - vi])
+              if abs(x.imag) < 1e-10 and -1e-12 <= x.real <= x_turn + 1e-12]
+    if len(branch) != 1:
+        raise RuntimeError(f"SI Eq. S7a has no unique physical root for v_i={vi}")
+    return float(branch[0] / rho ** (1.0 / 3.0))
 
 
 def _reference_default_path() -> Path:

@@ -82,13 +82,13 @@ def test_config_accepts_periodic_and_validates():
 def test_analytic_values_vs_reference(golden):
     an = json.loads((ROOT / "tests" / "golden" / "analytic.json").read_text())
     for vi, rho, a in an["alpha_star"]:
-        assert E.alpha_star_from_vi(vi, rho) == pytest.approx(a, rel=1e-12, abs=1e-15)
+        assert E.alpha_star_from_vi(vi, rho) == a          # the reference's arithmetic, bit for bit
     c0 = SimConfig(ts=0.01, T_max_ms=46.0, small_deltas=[6.0], big_deltas=[15.0, 25.0, 30.0, 40.0],
                    b_values=[0.0, 1000.0, 2500.0, 4000.0, 6000.0])
     for vi, rho, av in an["mean_AV"]:
-        assert E.governing_mean_A_over_V(vi, rho, c0)[0] == pytest.approx(av, rel=1e-14)
+        assert E.governing_mean_A_over_V(vi, rho, c0)[0] == av
     for rho, tm, side in an["si_domain_side"]:
-        assert E.si_domain_side_um(rho, SimConfig(T_max_ms=tm, small_deltas=[1.0], big_deltas=[1.0])) == pytest.approx(side, rel=1e-14)
+        assert E.si_domain_side_um(rho, SimConfig(T_max_ms=tm, small_deltas=[1.0], big_deltas=[1.0])) == side
     from custom_madi_gb300 import walker_gpu as W
     from custom_madi_gb300 import signal as S
     for k, av, pp in an["kio_to_pp"]:
@@ -234,3 +234,37 @@ def test_stage_block_refuses_offsets_past_32_bits():
     assert int(stage_offsets([16, 16, 16, 2 ** 32 - 16 * 4, 0, 0, 0])[-1]) == 2 ** 32 - 16
     with pytest.raises(N.MadiError):
         stage_offsets([16, 16, 16, 2 ** 32 - 16 * 3, 0, 0, 0])      # each part under the limit, the sum at it
+
+
+@pytest.mark.parametrize("rho,V,n_cells,seed", [(2.0e5, 4.0, 64, 0), (5.39597446e7, 0.0152563555, 486, 10),
+                                               (4484.29, 177.71676748, 31, 161)])
+def test_oracle_geometry_restatement_equals_product_builder(rho, V, n_cells, seed):
+    """The oracle's host-only periodic ensemble (the reference arm's geometry)
+    draws the package's seeds and annuli bit for bit, with the same alpha*,
+    <A/V> and Eq. 5 p_p; its KD build equals the native builder on the same
+    distinct-coordinate seeds (a tiled set has exact coordinate ties, where
+    the median element is the selection algorithm's choice: both trees are
+    exact); and its 27-image classifier set labels points exactly as the
+    package's proven-margin set and as the all-seed rule do."""
+    from dataclasses import replace
+    from custom_madi_gb300 import workloads as WL
+    from custom_madi_gb300.walker_gpu import kio_to_pp
+    from oracle import geometry as OG
+    cfg = replace(WL.batch_config(n_walkers=1000), n_cells=n_cells)
+    ens = E.create_ensemble(rho, V, cfg, seed=seed, verify_vi=False, measure_vi=False)
+    og = OG.periodic_ensemble(rho, V, n_cells, seed)
+    assert np.array_equal(og["seeds"], ens.seeds) and np.array_equal(og["annulus"], ens.annulus)
+    assert og["L"] == ens.L and og["alpha_star"] == pytest.approx(ens.alpha_star, rel=1e-12)
+    assert og["mean_AV"] == pytest.approx(ens.mean_AV, rel=1e-14)
+    assert OG.kio_to_pp(20.0, og["mean_AV"], cfg.D0, cfg.ts) == pytest.approx(kio_to_pp(20.0, ens.mean_AV, cfg),
+                                                                              rel=1e-13)
+    for a, b in zip(OG.kd_build(og["seeds"]), E._build_gpu_kdtree(og["seeds"])):
+        assert np.array_equal(a, b)
+    pts = np.random.default_rng(seed + 1).uniform(0.0, ens.L, (3000, 3))
+    geo = OG.oracle_geometry(og)
+    c_o, i_o = O.classify_kd(geo, pts)
+    c_p, i_p = O.classify_kd(O.geom_arrays(ens), pts)
+    c_b, i_b = O.classify_brute(geo, pts)
+    assert np.array_equal(c_o, c_p) and np.array_equal(i_o, i_p)
+    assert np.array_equal(c_o, c_b) and np.array_equal(i_o, i_b)
+    assert 0.0 < i_o.mean() < 1.0
