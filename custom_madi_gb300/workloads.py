@@ -7,9 +7,14 @@
 * batch_triplets(): 256 (kio, rho, V) drawn log-uniform from kio 1-130 1/s,
   rho 4.4e3-5.8e7 cells/uL, V 0.01-206 pL with 0.5 <= v_i <= 0.99 (the build's
   hard ceiling), periodic boxes of 27-512 cells, 1e5 walkers per entry.
+* walker_library(): the 20,000 x 20 fitting library walked by the batched
+  walker over the same (kio, rho, V) ranges: 2,000 (rho, V) geometries (64-cell
+  periodic boxes) x 10 kio each, direction-averaged over 24 directions and
+  normalised to b = 0 (S = 1 there exactly).
+* mixed_triplets(): the large mixed workload's entries (cells 27-1024).
 * match_library() / rician_voxels(): a 20,000 x 20 library of smooth
-  direction-averaged decays normalised to b = 0 and 1e6 voxels drawn from it
-  with Rician noise at SNR 30.
+  direction-averaged decays normalised to b = 0 (kernel tests), and voxels
+  drawn from a library with Rician noise at SNR 30.
 """
 
 from __future__ import annotations
@@ -105,3 +110,55 @@ def two_delta_columns(seed: int = 3) -> np.ndarray:
     rng = np.random.default_rng(seed + 2)
     d = np.sort(rng.choice(4, 2, replace=False))
     return np.concatenate([np.arange(5) + 5 * k for k in d])
+
+
+def mixed_triplets(n: int = 140, seed: int = 4) -> List[Tuple[float, float, float, int]]:
+    """Entries of the large mixed workload: batched-build ranges, 27-1024 cells."""
+    return batch_triplets(n, seed=seed, cells=(27, 1024))
+
+
+def walker_library(n_groups: int = 2000, kios_per_group: int = 10, n_walkers: int = 4096, seed: int = 3,
+                   threads: int = 8, device=None, launch=None) -> Tuple[np.ndarray, np.ndarray, dict]:
+    """(lib [n_groups * kios_per_group, 20] fp64, params [n, 3] (kio, rho, V), info).
+
+    (rho, V) pairs are drawn like batch_triplets (log-uniform, 0.5 <= v_i <=
+    0.99); each gets one 64-cell periodic geometry walked at kios_per_group kio
+    values log-uniform in [1, 130] (the reference's kio sweep reuses a
+    geometry: madi/library.py:483-520).  All walks run in one persistent launch;
+    every entry is S averaged over 24 Fibonacci directions, 4 Delta x 5 b,
+    pair-major, so S = 1 at b = 0.
+    """
+    import time
+    from .walker_gpu import LaunchConfig, WalkBatch, WalkJob, _walk_seed, kio_to_pp, pair_layout
+    from . import signal as S
+    rng = np.random.default_rng(seed + 7)
+    groups = batch_triplets(n_groups, seed=seed + 11)
+    kios = np.sort(np.exp(rng.uniform(np.log(1.0), np.log(130.0), (n_groups, kios_per_group))), axis=1)
+    cfg = batch_config(n_walkers=n_walkers)
+    t0 = time.perf_counter()
+    ens = build_ensembles([(1.0, r, v, 64) for _k, r, v, _n in groups], cfg, seed=seed * 100_000, threads=threads)
+    t_host = time.perf_counter() - t0
+    cols = S.build_columns(cfg)
+    lay = pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    u = cfg.direction_array()
+    jobs, params = [], []
+    for g, e in enumerate(ens):
+        for k in kios[g]:
+            jobs.append(WalkJob(e, kio_to_pp(float(k), e.mean_AV, cfg), _walk_seed(seed, g), n_walkers))
+            params.append((float(k), groups[g][1], groups[g][2]))
+    import torch
+    t0 = time.perf_counter()
+    batch = WalkBatch(jobs, cfg, layout=lay, dirs=u, launch=launch or LaunchConfig(), device=device)
+    batch.launch()
+    torch.cuda.synchronize(batch.dev)
+    t_walk = time.perf_counter() - t0
+    res = batch.results()
+    lib = np.stack([r["cos"].sum(axis=1) for r in res]) / float(len(u) * n_walkers)
+    lib /= lib[:, [0]]
+    cnt = batch.counters_np()
+    if int(cnt[:, 1].sum()) or int(cnt[:, 2].sum()):
+        raise RuntimeError("walker library: escaped walkers or classifier errors")
+    info = {"entries": len(jobs), "geometries": len(ens), "walkers_per_entry": n_walkers,
+            "walker_steps": len(jobs) * n_walkers * cfg.n_steps, "host_geometry_s": t_host,
+            "walk_s": t_walk}
+    return lib, np.asarray(params, np.float64), info
