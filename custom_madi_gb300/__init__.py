@@ -1,7 +1,7 @@
 """GB300-native MADI Monte Carlo diffusion hot path (drop-in for the reference's madi package).
 
 Submodules mirror the reference package: config, ensemble, walker_gpu, signal,
-library, fitters_gpu.  Compute runs in hand-written sm_103a CUDA
+library, fitters_gpu, fitters.  Compute runs in hand-written sm_103a CUDA
 kernels behind the C ABI of include/madi_gb300.h (loaded by _native.py on first
 use; importing the package loads no native code).
 
@@ -17,11 +17,12 @@ from . import walker_gpu  # noqa: F401
 from . import signal  # noqa: F401
 from . import library  # noqa: F401
 from . import fitters_gpu  # noqa: F401
+from . import fitters  # noqa: F401
 
-__all__ = ["config", "ensemble", "walker_gpu", "signal", "library", "fitters_gpu", "install_madi_alias"]
+__all__ = ["config", "ensemble", "walker_gpu", "signal", "library", "fitters_gpu", "fitters", "install_madi_alias"]
 __version__ = "0.2.0"
 
-_ALIASED = ("config", "ensemble", "walker_gpu", "signal", "library", "fitters_gpu")
+_ALIASED = ("config", "ensemble", "walker_gpu", "signal", "library", "fitters_gpu", "fitters")
 
 
 def install_madi_alias(name: str = "madi") -> None:

@@ -21,7 +21,7 @@ LIBDIR = PKG / "_lib"
 OBJDIR = LIBDIR / "obj"
 LIBNAME = "libmadi_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["walk.cu", "classify.cu", "match.cu", "match_bf16.cu"]
+CU_SOURCES = ["walk.cu", "classify.cu", "match.cu", "match_bf16.cu", "bayes.cu"]
 CPP_SOURCES = ["host.cpp", "serve.cpp"]
 
 

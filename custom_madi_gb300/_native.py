@@ -45,6 +45,7 @@ MADI_CNT_N = len(CNT_NAMES)
 EXPORTED = (
     "madi_abi_version", "madi_last_error_string", "madi_classify", "madi_walk",
     "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_wait", "madi_match_scratch_bytes",
+    "madi_bayes", "madi_bayes_scratch_bytes",
     "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_walk_blocks_per_sm", "madi_walk_noalloc",
     "madi_walk_batched", "madi_autotune_load", "madi_autotune_store",
     "madi_serve_arena_bytes", "madi_serve_create", "madi_serve_submit", "madi_serve_poll",
@@ -114,6 +115,18 @@ class MadiMatchDesc(C.Structure):
     ]
 
 
+class MadiBayesDesc(C.Structure):
+    _fields_ = [
+        ("measured", C.c_void_p), ("lib", C.c_void_p), ("log_weight", C.c_void_p), ("kio", C.c_void_p),
+        ("rho", C.c_void_p), ("V", C.c_void_p), ("n_vox", C.c_int64), ("n_lib", C.c_int32),
+        ("n_feat", C.c_int32), ("mode", C.c_int32), ("pad0", C.c_int32), ("sigma_m", C.c_double),
+        ("out", C.c_void_p), ("scratch", C.c_void_p), ("scratch_bytes", C.c_int64),
+    ]
+
+
+MADI_BAYES_N_OUT = 9
+
+
 class MadiServeConfig(C.Structure):
     _fields_ = [("walk", MadiWalkDesc), ("n_slots", C.c_int32), ("chunk_walkers", C.c_int32),
                 ("launch_walkers", C.c_int32), ("inflight", C.c_int32), ("budget_bytes", C.c_int64),
@@ -165,6 +178,9 @@ def _declare(lib):
     lib.madi_reduce_Y.argtypes = [P, C.c_int64, C.c_int32, P, P, P, P, C.c_int32, P, P, P]
     lib.madi_match.argtypes = [C.POINTER(MadiMatchDesc), P]
     lib.madi_match_wait.argtypes = [C.POINTER(MadiMatchDesc), P]
+    lib.madi_bayes.argtypes = [C.POINTER(MadiBayesDesc), P]
+    lib.madi_bayes_scratch_bytes.argtypes = [C.c_int32, C.c_int32]
+    lib.madi_bayes_scratch_bytes.restype = C.c_int64
     lib.madi_match_scratch_bytes.argtypes = [C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     lib.madi_match_scratch_bytes.restype = C.c_int64
     lib.madi_kdtree_build.argtypes = [P, C.c_int32, P, P, P, P, P]
@@ -173,7 +189,7 @@ def _declare(lib):
     lib.madi_facets_build.argtypes = [P, C.c_int32, C.c_int32, C.c_double, P, P, P, C.c_int64,
                                       C.POINTER(C.c_int64), P]
     for name in ("madi_classify", "madi_walk", "madi_walk_noalloc", "madi_walk_batched", "madi_reduce_Y",
-                 "madi_match", "madi_match_wait", "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_autotune_load",
+                 "madi_match", "madi_match_wait", "madi_bayes", "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_autotune_load",
                  "madi_autotune_store", "madi_serve_create", "madi_serve_submit", "madi_serve_poll",
                  "madi_serve_release", "madi_serve_destroy"):
         getattr(lib, name).restype = C.c_int

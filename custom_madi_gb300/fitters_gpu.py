@@ -117,3 +117,53 @@ def map_match_fits0_gpu(raw_signal, lib_mat, kios_arr, rhos_arr, Vs_arr, *, prec
     b = _indices(idx)
     return (np.asarray(kios_arr)[b], np.asarray(rhos_arr)[b], np.asarray(Vs_arr)[b],
             res.cpu().numpy().astype(np.float64), s0.cpu().numpy().astype(np.float64))
+
+
+def bayes_fit_gpu(measured_batch, lib_mat, kios_arr, rhos_arr, Vs_arr, sigma_m, fit_s0=False,
+                  quadrature_weights=None, *, stream=None) -> dict:
+    """GPU Bayesian posterior means (madi/fitters_gpu.py:466-528 signature).
+
+    ``measured_batch`` is the normalised (and, if asked, log-transformed)
+    signal for fixed S0 or the raw signal for ``fit_s0=True``.  Returns
+    kio/rho/V means and stds, the weighted residual and n_eff (+ s0_fit) as
+    fp64 numpy arrays; one ``madi_bayes`` launch.
+    """
+    if not HAS_CUDA:
+        raise RuntimeError("CUDA is unavailable: the Bayesian fit runs on a CUDA device only")
+    if quadrature_weights is None:
+        raise ValueError("Bayesian GPU fitting requires positive quadrature weights.")
+    q = np.ascontiguousarray(quadrature_weights, dtype=np.float64)
+    kios_arr = np.asarray(kios_arr, np.float64)
+    if q.shape != kios_arr.shape or not np.all(np.isfinite(q) & (q > 0.0)):
+        raise ValueError("invalid Bayesian quadrature weights")
+    if not (float(sigma_m) > 0.0):
+        raise ValueError(f"sigma_m must be > 0, got {sigma_m}")
+    M = _as_dev(measured_batch)
+    Lm = _as_dev(lib_mat)
+    if M.ndim != 2 or Lm.ndim != 2 or M.shape[1] != Lm.shape[1]:
+        raise ValueError("measured (n_vox, F) and library (n_lib, F) must share F")
+    dev = M.device
+    n_vox, F = M.shape
+    n_lib = Lm.shape[0]
+    par = [torch.from_numpy(np.ascontiguousarray(a, np.float64)).to(dev)
+           for a in (np.log(q), kios_arr, np.asarray(rhos_arr, np.float64), np.asarray(Vs_arr, np.float64))]
+    out = torch.empty((N.MADI_BAYES_N_OUT, n_vox), dtype=torch.float64, device=dev)
+    scratch = torch.empty(int(N.lib().madi_bayes_scratch_bytes(n_lib, F)) + 256, dtype=torch.uint8, device=dev)
+    d = N.MadiBayesDesc()
+    d.measured, d.lib = N.ptr(M), N.ptr(Lm)
+    d.log_weight, d.kio, d.rho, d.V = (N.ptr(t) for t in par)
+    d.n_vox, d.n_lib, d.n_feat = n_vox, n_lib, F
+    d.mode = N.MADI_MATCH_FREE_S0 if fit_s0 else N.MADI_MATCH_FIXED_S0
+    d.sigma_m = float(sigma_m)
+    d.out = N.ptr(out)
+    base = N.ptr(scratch)
+    pad = (-base) % 256
+    d.scratch, d.scratch_bytes = base + pad, int(scratch.numel()) - pad
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    N.check(N.lib().madi_bayes(C.byref(d), s.cuda_stream), "madi_bayes")
+    o = out.cpu().numpy()
+    res = dict(kio_mean=o[0], rho_mean=o[1], V_mean=o[2], kio_std=o[3], rho_std=o[4], V_std=o[5],
+               residual=o[6], n_eff=o[7])
+    if fit_s0:
+        res["s0_fit"] = o[8]
+    return res

@@ -304,6 +304,44 @@ madi_status madi_match(const madi_match_desc* desc, void* stream);
 madi_status madi_match_wait(const madi_match_desc* desc, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Bayesian posterior-mean fit (madi/fitters.py:110-243, the two-pass kernels  */
+/* of madi/fitters_gpu.py:156-294 and bayes_fit_gpu :466-528)               */
+/* ------------------------------------------------------------------------ */
+
+/* Per voxel, entry j weighs w_j = q_j exp(-rw_j / (2 sigma_m^2)) with rw_j the
+ * normalised residual (fixed S0: |m - L_j|^2; free S0: |m/s0_j - L_j|^2 with
+ * s0_j = m.L_j / |L_j|^2, entries with s0_j <= 0 weigh 0); q_j = exp(log_weight[j]).
+ * out: device fp64 [MADI_BAYES_N_OUT][n_vox] = kio, rho, V posterior means,
+ * their standard deviations, the weighted residual (raw units for free S0),
+ * n_eff = (sum w)^2 / sum w^2 and (free S0) the weighted S0.  A free-S0 voxel
+ * that no entry fits with s0 > 0 gets zeros.  Entries whose weight is below
+ * e^-60 of the voxel's largest weight are dropped.  Arithmetic: fp32 scores
+ * screen the entries; the kept ones get a direct-difference fp32 residual
+ * (error ~F ulp of the residual) and Kahan-compensated fp32 sums of
+ * parameter differences from the best entry, combined in fp64.
+ * scratch: 256-byte aligned, madi_bayes_scratch_bytes() bytes. */
+#define MADI_BAYES_N_OUT 9
+typedef struct madi_bayes_desc {
+    const float* measured;         /* [n_vox][n_feat] (fixed: normalised; free: raw) */
+    const float* lib;              /* [n_lib][n_feat]               */
+    const double* log_weight;      /* [n_lib] log quadrature weight */
+    const double* kio;             /* [n_lib]                       */
+    const double* rho;             /* [n_lib]                       */
+    const double* V;               /* [n_lib]                       */
+    int64_t n_vox;
+    int32_t n_lib, n_feat;
+    int32_t mode;                  /* MADI_MATCH_FIXED_S0 / FREE_S0 */
+    int32_t pad0;
+    double sigma_m;
+    double* out;                   /* [MADI_BAYES_N_OUT][n_vox]     */
+    void* scratch;
+    int64_t scratch_bytes;
+} madi_bayes_desc;
+
+int64_t madi_bayes_scratch_bytes(int32_t n_lib, int32_t n_feat);
+madi_status madi_bayes(const madi_bayes_desc* desc, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Host-side geometry builders (native C++; no device work)                 */
 /* ------------------------------------------------------------------------ */
 

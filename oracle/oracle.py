@@ -225,3 +225,44 @@ def match_free(raw, lib_mat, chunk: int = 20_000) -> tuple[np.ndarray, np.ndarra
         rows = np.arange(len(b))
         idx[s:s + chunk], res[s:s + chunk], s0[s:s + chunk] = b, r[rows, b], cand[rows, b]
     return idx, res, s0
+
+
+def bayes(measured, lib_mat, kios, rhos, Vs, weights, sigma_m, fit_s0=False, chunk: int = 4000) -> dict:
+    """fp64 Bayesian posterior means (madi/fitters.py:159-243): log-weights
+    log q - r / (2 sigma_m^2), shifted by their row maximum, normalised; free S0
+    uses the raw residual |m|^2 - (m.r)^2/|r|^2 divided by S0^2 for the weight
+    and masks S0 <= 0; rows with no admissible entry give zeros."""
+    M = np.asarray(measured, np.float64)
+    R = np.asarray(lib_mat, np.float64)
+    lq = np.log(np.asarray(weights, np.float64))[None, :]
+    k, r_, v = (np.asarray(a, np.float64) for a in (kios, rhos, Vs))
+    keys = ("kio_mean", "rho_mean", "V_mean", "kio_std", "rho_std", "V_std", "residual", "n_eff") + \
+        (("s0_fit",) if fit_s0 else ())
+    out = {key: np.empty(len(M)) for key in keys}
+    for s in range(0, len(M), chunk):
+        m = M[s:s + chunk]
+        if fit_s0:
+            rr = np.maximum(np.sum(R * R, axis=1), 1e-30)
+            mr = m @ R.T
+            s0 = mr / rr[None, :]
+            resid = np.sum(m * m, axis=1)[:, None] - mr ** 2 / rr[None, :]
+            resid = np.where(s0 > 0, resid, np.inf)
+            wres = resid / np.where(s0 > 0, s0, 1.0) ** 2
+        else:
+            resid = np.maximum(np.sum(m * m, axis=1)[:, None] + np.sum(R * R, axis=1)[None, :] - 2.0 * m @ R.T, 0.0)
+            wres = resid
+        lw = lq - wres / (2.0 * sigma_m ** 2)
+        mx = np.max(lw, axis=1, keepdims=True)
+        bad = ~np.isfinite(mx)
+        w = np.where(bad, 0.0, np.exp(lw - np.where(bad, 0.0, mx)))
+        w /= np.maximum(np.sum(w, axis=1, keepdims=True), 1e-300)
+        sl = slice(s, s + len(m))
+        for name, vals in (("kio", k), ("rho", r_), ("V", v)):
+            mean = w @ vals
+            out[f"{name}_mean"][sl] = mean
+            out[f"{name}_std"][sl] = np.sqrt(np.maximum(w @ vals ** 2 - mean ** 2, 0.0))
+        out["residual"][sl] = np.sum(w * np.where(np.isfinite(resid), resid, 0.0), axis=1)
+        out["n_eff"][sl] = np.where(bad[:, 0], 0.0, 1.0 / np.maximum(np.sum(w ** 2, axis=1), 1e-300))
+        if fit_s0:
+            out["s0_fit"][sl] = np.sum(w * s0, axis=1)
+    return out

@@ -10,7 +10,7 @@ tests read; nothing at test time imports the reference.
 
 ``base`` writes the classifier, walk, matcher, analytic, population and
 library fixtures; ``api`` the host-API fixtures (random stream, result merge,
-Bayes fit).  Without ``--only`` both are written.
+Bayes fit: api.npz, bayes.npz).  Without ``--only`` both are written.
 """
 
 from __future__ import annotations
@@ -238,7 +238,7 @@ def base_fixtures() -> None:
 
 
 def api_fixtures() -> None:
-    """Host-API vectors: make_walk_random_stream's draws, _merge_results order."""
+    """Host-API vectors: make_walk_random_stream's draws, _merge_results order, bayes_fit."""
     config, E, W, S, Lb = _import_reference()
     # ---- 10. make_walk_random_stream (madi/walker_gpu.py:115-127) -------------------
     scfg = config.SimConfig(L=30.0, n_walkers=5, n_ensembles=1, ts=0.01, T_max_ms=0.04, h_ms=0.01,
@@ -256,6 +256,30 @@ def api_fixtures() -> None:
             ensemble_cos_means=[rng.normal(size=4)], ensemble_sin_means=[rng.normal(size=4)],
             classifier_cache_stats=[{"full": e}]))
     m = W._merge_results(parts)
+    # ---- 12. bayes_fit, CPU path of the reference (madi/fitters.py:110-243) ---------
+    from madi import fitters as Fi
+    r12 = np.random.default_rng(12)
+    n_lib, n_feat = 300, 10
+    Dv = r12.uniform(0.2, 3.0, n_lib)[:, None]
+    bgrid = np.linspace(0.0, 3.0, n_feat)[None, :]
+    bmat = np.exp(-bgrid * Dv) * r12.uniform(0.85, 1.0, (n_lib, 1))
+    bkio, brho, bV = r12.uniform(1, 100, n_lib), r12.uniform(1e5, 1e6, n_lib), r12.uniform(0.6, 0.9, n_lib)
+    bq = r12.uniform(0.5, 2.0, n_lib)
+    bents = [Lb.LibraryEntry(float(bkio[i]), float(brho[i]), float(bV[i] * 1e6 / brho[i]), bmat[i],
+                             vi=float(bV[i]), weight=float(bq[i])) for i in range(n_lib)]
+    bpairs, bbv = [(10.0, 20.0)], list(np.arange(n_feat) * 500.0)
+    btrip = [(10.0, 20.0, b) for b in bbv]
+    bmeas = bmat[r12.integers(0, n_lib, 400)] + 0.02 * r12.normal(size=(400, n_feat))
+    braw = bmeas * r12.uniform(50.0, 2000.0, (400, 1))
+    kw = dict(lib_delta_pairs=bpairs, lib_b_values=bbv, n_b=n_feat, fit_triples=btrip, vi_min=0.5, vi_max=0.95,
+              use_gpu=False)
+    bfix = Fi.bayes_fit(bmeas, bents, sigma_m=0.03, **kw)
+    bfree = Fi.bayes_fit(bmeas, bents, sigma_m=0.03, fit_s0=True, raw_signal=braw, **kw)
+    bayes = {f"bayes_fixed_{k}": v for k, v in bfix.items()}
+    bayes.update({f"bayes_free_{k}": v for k, v in bfree.items()})
+    np.savez_compressed(
+        HERE / "bayes.npz", lib=bmat, kio=bkio, rho=brho, V=np.array([e.V for e in bents]), vi=bV, weight=bq,
+        measured=bmeas, raw=braw, bvals=np.array(bbv), sigma_m=0.03, **bayes)
     np.savez_compressed(
         HERE / "api.npz", stream_seed=424242, stream_n_walkers=5, stream_n_steps=scfg.n_steps,
         stream_L=30.0, stream_source_lo=dummy.source_lo, stream_source_hi=dummy.source_hi,

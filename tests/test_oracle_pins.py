@@ -35,8 +35,8 @@ def test_oracle_periodic_classifier_on_27_images(golden):
     tiled = (base[None] + shifts[:, None]).reshape(-1, 3)
     ann = np.tile(d["annulus"], 27)
     cell = np.tile(np.arange(64, dtype=np.int32), 27)
-    from custom_madi_gb300.ensemble import _build_gpu_kdtree  # native host builder, no GPU work
-    kd = _build_gpu_kdtree(tiled)
+    from oracle.geometry import kd_build        # the oracle's own KD build
+    kd = kd_build(tiled)
     g = O.Geometry(tiled, ann, kd, L, cell=cell, periodic=True)
     c, i = O.classify_brute(g, d["points"])
     assert np.array_equal(i, d["inside"]) and np.array_equal(c, d["cell"])
@@ -102,3 +102,14 @@ def test_oracle_matcher_tie_picks_lowest_index():
     lib = np.array([[0.8, 0.5, 0.3], [0.8, 0.5, 0.3], [0.7, 0.4, 0.2]])
     idx, _ = O.match_fixed(np.array([[0.8, 0.5, 0.3], [0.71, 0.39, 0.19]]), lib)
     assert idx.tolist() == [0, 2]
+
+
+def test_oracle_bayes_matches_reference_bayes_fit(golden):
+    """The oracle's fp64 Bayesian fit equals the reference bayes_fit
+    (madi/fitters.py:110-243, CPU path) on its fixture, fixed and free S0."""
+    from oracle import oracle as O
+    b = golden("bayes.npz")
+    for mode, meas, free in (("fixed", b["measured"], False), ("free", b["raw"], True)):
+        got = O.bayes(meas, b["lib"], b["kio"], b["rho"], b["V"], b["weight"], float(b["sigma_m"]), fit_s0=free)
+        for key, val in got.items():
+            np.testing.assert_allclose(val, b[f"bayes_{mode}_{key}"], rtol=1e-9, atol=1e-12, err_msg=f"{mode} {key}")
