@@ -10,7 +10,8 @@ tests read; nothing at test time imports the reference.
 
 ``base`` writes the classifier, walk, matcher, analytic, population and
 library fixtures; ``api`` the host-API fixtures (random stream, result merge,
-Bayes fit: api.npz, bayes.npz).  Without ``--only`` both are written.
+Bayes fit, shard merge: api.npz, bayes.npz, shards/).  Without ``--only`` both
+are written.
 """
 
 from __future__ import annotations
@@ -275,6 +276,38 @@ def api_fixtures() -> None:
               use_gpu=False)
     bfix = Fi.bayes_fit(bmeas, bents, sigma_m=0.03, **kw)
     bfree = Fi.bayes_fit(bmeas, bents, sigma_m=0.03, fit_s0=True, raw_signal=braw, **kw)
+    # ---- 13. shard merge by the reference's own script (scripts/merge_shards.py) ------
+    import subprocess
+    sdir = HERE / "shards"
+    sdir.mkdir(exist_ok=True)
+    for old in sdir.glob("*.npz"):
+        old.unlink()
+    mcfg = config.SimConfig(n_walkers=2, n_ensembles=2, small_deltas=[5.0, 7.0, 10.0, 12.0, 15.0, 20.0, 25.0, 30.0],
+                            big_deltas=[15.0, 25.0, 30.0, 36.0, 40.0, 50.0, 60.0, 80.0])
+    mcols = S.build_columns(mcfg)
+    mnc = mcols.n_pairs * mcols.n_b
+    msub = Lb.ensemble_mean_subset_column_indices(mcols)
+    r13 = np.random.default_rng(13)
+
+    def entry(k, rho, V, free=False):
+        vec = np.linspace(1.0, 0.05 + 0.001 * k, mnc)
+        em = (vec[None, :] + r13.normal(0.0, 0.01, (2, mnc))).astype(np.float32)
+        return Lb.LibraryEntry(kio=float("nan") if free else k, rho=0.0 if free else rho, V=0.0 if free else V,
+                               vector=vec, signal_imag=r13.normal(0, 1e-3, mnc).astype(np.float32),
+                               signal_variance=np.full(mnc, 1e-4, np.float32), ensemble_means_subset=em[:, msub],
+                               vi=0.0 if free else rho * V * 1e-6, weight=1.0 + k / 100.0, kio_nominal=k,
+                               rho_nominal=rho, V_nominal=V, pp=0.01, kio_analytic_eq5=k, is_free_water=free,
+                               metadata={"k": k})
+    shard_sets = [[entry(5.0, 2e5, 4.0), entry(10.0, 2e5, 4.0), entry(0.0, 0.0, 0.0, free=True)],
+                  [entry(10.0, 2e5, 4.0), entry(15.0, 3e5, 2.0), entry(0.0, 0.0, 0.0, free=True)],
+                  [entry(20.0, 3e5, 2.0), entry(5.0, 2e5, 4.0), entry(25.0, 1e5, 5.5)]]
+    for i, ents in enumerate(shard_sets):
+        Lb._save_library(ents, str(sdir / f"lib.shard{i}.npz"), cfg=mcfg, columns=mcols, build_seed=3,
+                         grid_metadata={"kind": "shard fixture"})
+    env = dict(os.environ, PYTHONPATH=os.pathsep.join(sys.path))
+    subprocess.run([sys.executable, str(REFERENCE_ROOT / "scripts" / "merge_shards.py"),
+                    *[str(sdir / f"lib.shard{i}.npz") for i in range(3)], "-o", str(sdir / "merged_by_reference.npz"),
+                    "--require-shards", "3"], check=True, env=env, stdout=subprocess.DEVNULL)
     bayes = {f"bayes_fixed_{k}": v for k, v in bfix.items()}
     bayes.update({f"bayes_free_{k}": v for k, v in bfree.items()})
     np.savez_compressed(
