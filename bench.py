@@ -363,6 +363,7 @@ def main(argv=None):
             sec["serving"] = serving_legs(dev, args.serving_requests, lib, threads)
         if not args.no_mixed:
             sec["mixed"] = mixed_leg(dev, lib, threads)
+        sec["reduce_production_grid"] = reduce_leg(dev)
         line["secondary"] = sec
     if rank == 0:
         print(json.dumps(line))
@@ -634,6 +635,49 @@ def mixed_leg(dev, lib, threads):
             "extrapolated_14000_entries_plain_h": full_steps / plain_rate / 3600.0,
             "extrapolation": "time for 14,000 entries = 6.44e13 walker-steps at the measured rate "
                              "(host geometry builds overlap the walk and are not included)"}
+
+
+def reduce_leg(dev):
+    """Column reduction of stored Y at the reference's production grid: 31,125
+    columns (1,245 (delta, Delta) pairs x 25 b), n_grid = 129 (T = 128 ms), 5e4
+    walkers (one ensemble of the production configuration); Y is a synthetic
+    Brownian trajectory integral of that shape.  The oracle's fp64 reduction
+    times 64 of the walkers on one host thread."""
+    import torch
+    from oracle import oracle as O
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.config import SimConfig
+    cfg = SimConfig(ts=0.01)
+    cols = S.build_columns(cfg)
+    n, ng = 50_000, cfg.n_grid
+    g = torch.Generator(device=dev).manual_seed(5)
+    x = torch.cumsum(torch.randn((n, ng, 3), generator=g, device=dev, dtype=torch.float64) * 1.7, dim=1)
+    Y = torch.cumsum(x, dim=1) * 1e-3
+    jd, jD, js = (torch.from_numpy(np.asarray(a, np.int32)).to(dev) for a in (cols.j_delta, cols.j_Delta, cols.j_sum))
+    pc = torch.from_numpy(np.asarray(cols.phase_coef, np.float64)).to(dev)
+    cs = torch.empty(len(pc), dtype=torch.float64, device=dev)
+    ss = torch.empty_like(cs)
+    st = torch.cuda.current_stream(dev)
+    N.reduce_Y(Y, n, ng, jd, jD, js, pc, cs, ss, st)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = []
+    for _ in range(3):
+        e0.record(st)
+        N.reduce_Y(Y, n, ng, jd, jD, js, pc, cs, ss, st)
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        times.append(e0.elapsed_time(e1))
+    t = min(times) / 1e3
+    y64 = Y[:64].cpu().numpy()
+    t0 = time.perf_counter()
+    oc, _ = O.reduce(y64, cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    t_cpu = time.perf_counter() - t0
+    terms = float(n) * len(pc) * 3
+    return {"columns": int(len(pc)), "walkers": n, "n_grid": ng, "ms": t * 1e3,
+            "walker_column_axis_terms_per_s": terms / t, "Y_bytes": int(Y.numel() * 8),
+            "cpu_oracle_terms_per_s_1_thread": 64.0 * len(pc) * 3 / t_cpu,
+            "note": "Y read once per block of 1,024 columns (31 blocks), fp64 sincos per term"}
 
 
 if __name__ == "__main__":

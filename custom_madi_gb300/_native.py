@@ -44,7 +44,7 @@ MADI_CNT_N = len(CNT_NAMES)
 
 EXPORTED = (
     "madi_abi_version", "madi_last_error_string", "madi_classify", "madi_walk",
-    "madi_walk_smem_bytes", "madi_reduce_Y", "madi_match", "madi_match_wait", "madi_match_scratch_bytes",
+    "madi_walk_smem_bytes", "madi_reduce_Y", "madi_reduce_Y_scratch_bytes", "madi_match", "madi_match_wait", "madi_match_scratch_bytes",
     "madi_bayes", "madi_bayes_scratch_bytes",
     "madi_kdtree_build", "madi_grid_build", "madi_facets_build", "madi_walk_blocks_per_sm", "madi_walk_noalloc",
     "madi_walk_batched", "madi_autotune_load", "madi_autotune_store",
@@ -175,7 +175,9 @@ def _declare(lib):
     lib.madi_walk_smem_bytes.restype = C.c_int64
     lib.madi_walk_blocks_per_sm.argtypes = [C.POINTER(MadiWalkDesc)]
     lib.madi_walk_blocks_per_sm.restype = C.c_int32
-    lib.madi_reduce_Y.argtypes = [P, C.c_int64, C.c_int32, P, P, P, P, C.c_int32, P, P, P]
+    lib.madi_reduce_Y.argtypes = [P, C.c_int64, C.c_int32, P, P, P, P, C.c_int32, P, P, P, C.c_int64, P]
+    lib.madi_reduce_Y_scratch_bytes.argtypes = [C.c_int32]
+    lib.madi_reduce_Y_scratch_bytes.restype = C.c_int64
     lib.madi_match.argtypes = [C.POINTER(MadiMatchDesc), P]
     lib.madi_match_wait.argtypes = [C.POINTER(MadiMatchDesc), P]
     lib.madi_bayes.argtypes = [C.POINTER(MadiBayesDesc), P]
@@ -244,3 +246,14 @@ def ptr(t) -> int:
     if t is None:
         return 0
     return int(t.data_ptr())
+
+
+def reduce_Y(Y, n_walkers: int, n_grid: int, jd, jD, js, coef, cos_sum, sin_sum, stream) -> None:
+    """madi_reduce_Y on device tensors (int32 jd / jD / js, fp64 coef and outputs),
+    with a scratch buffer of the size the library asks for."""
+    import torch
+    n = int(coef.numel())
+    scratch = torch.empty(max(int(lib().madi_reduce_Y_scratch_bytes(n)) // 8, 1), dtype=torch.int64, device=coef.device)
+    st = lib().madi_reduce_Y(ptr(Y), int(n_walkers), int(n_grid), ptr(jd), ptr(jD), ptr(js), ptr(coef), n,
+                             ptr(cos_sum), ptr(sin_sum), ptr(scratch), scratch.numel() * 8, stream.cuda_stream)
+    check(st, "madi_reduce_Y")

@@ -745,39 +745,81 @@ __global__ void __launch_bounds__(128) walk_f64_kernel(const madi_walk_desc d) {
 }
 
 // ---------------------------------------------------------------------------
-// Column reduction from stored Y (madi/walker_gpu.py:658-695): one CTA per
-// column, fp64 partials, deterministic tree.
+// Column reduction from stored Y (replaces _reduce_kernel, madi/walker_gpu.py:
+// 658-695, which re-reads Y once per column).  A CTA takes a block of
+// REDUCE_THREADS * REDUCE_CPT columns and a range of walkers: walker rows are
+// staged in shared memory a few at a time and every thread adds, for its
+// columns, cos / sin(coef * dM) over the 3 axes with dM = Y[jd] + Y[jD] - Y[js]
+// (the reference's operation order) into fp64 partial sums in a fixed order.
+// Each (CTA, column) partial is then rounded once to 2^-32 fixed point and
+// added to an int64 accumulator: integer addition is order independent, so the
+// sums do not depend on how the grid was scheduled.  Y is read from HBM/L2
+// ceil(n_cols / (REDUCE_THREADS * REDUCE_CPT)) times instead of n_cols times.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) reduce_Y_kernel(const double* __restrict__ Y, int64_t n_walkers, int n_grid,
-                                                        const int32_t* jd, const int32_t* jD, const int32_t* js,
-                                                        const double* coef, double* cos_sum, double* sin_sum) {
-    __shared__ double sc[256], ss[256];
-    const int col = blockIdx.x;
-    const int a = jd[col], b = jD[col], c = js[col];
-    const double pc = coef[col];
-    double lc = 0.0, ls = 0.0;
-    const int64_t total = n_walkers * 3;
-    for (int64_t i = threadIdx.x; i < total; i += blockDim.x) {
-        const int64_t w = i / 3;
-        const int ax = (int)(i - 3 * w);
-        const double* y = Y + (size_t)w * n_grid * 3;
-        const double dm = y[3 * a + ax] + y[3 * b + ax] - y[3 * c + ax];
-        double s, cc;
-        sincos(pc * dm, &s, &cc);
-        lc += cc;
-        ls += s;
+constexpr int REDUCE_THREADS = 256;
+constexpr int REDUCE_CPT = 4;                                // columns per thread
+constexpr int REDUCE_COLS = REDUCE_THREADS * REDUCE_CPT;     // columns per CTA
+
+__global__ void __launch_bounds__(REDUCE_THREADS) reduce_Y_kernel(const double* __restrict__ Y, int64_t n_walkers,
+                                                                  int n_grid, int wt, int64_t per_block,
+                                                                  const int32_t* __restrict__ jd,
+                                                                  const int32_t* __restrict__ jD,
+                                                                  const int32_t* __restrict__ js,
+                                                                  const double* __restrict__ coef, int n_cols,
+                                                                  unsigned long long* accum) {
+    extern __shared__ double sy[];                            // [wt][n_grid * 3]
+    const int row_len = n_grid * 3;
+    int a[REDUCE_CPT], b[REDUCE_CPT], c[REDUCE_CPT];
+    double pc[REDUCE_CPT], cs[REDUCE_CPT], sn[REDUCE_CPT];
+#pragma unroll
+    for (int k = 0; k < REDUCE_CPT; ++k) {
+        const int col = blockIdx.x * REDUCE_COLS + k * REDUCE_THREADS + threadIdx.x;
+        const bool live = col < n_cols;
+        a[k] = live ? 3 * jd[col] : 0;
+        b[k] = live ? 3 * jD[col] : 0;
+        c[k] = live ? 3 * js[col] : 0;
+        pc[k] = live ? coef[col] : 0.0;
+        cs[k] = 0.0;
+        sn[k] = 0.0;
     }
-    sc[threadIdx.x] = lc;
-    ss[threadIdx.x] = ls;
-    __syncthreads();
-    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-        if ((int)threadIdx.x < st) {
-            sc[threadIdx.x] += sc[threadIdx.x + st];
-            ss[threadIdx.x] += ss[threadIdx.x + st];
-        }
+    const int64_t w0 = (int64_t)blockIdx.y * per_block;
+    const int64_t w1 = min(n_walkers, w0 + per_block);
+    for (int64_t wb = w0; wb < w1; wb += wt) {
+        const int nw = (int)min((int64_t)wt, w1 - wb);
         __syncthreads();
+        const double* src = Y + (size_t)wb * row_len;
+        for (int i = threadIdx.x; i < nw * row_len; i += REDUCE_THREADS) sy[i] = src[i];
+        __syncthreads();
+        for (int w = 0; w < nw; ++w) {
+            const double* y = sy + w * row_len;
+#pragma unroll
+            for (int k = 0; k < REDUCE_CPT; ++k) {
+#pragma unroll
+                for (int ax = 0; ax < 3; ++ax) {
+                    const double dm = __dsub_rn(__dadd_rn(y[a[k] + ax], y[b[k] + ax]), y[c[k] + ax]);
+                    double s, co;
+                    sincos(__dmul_rn(pc[k], dm), &s, &co);
+                    cs[k] += co;
+                    sn[k] += s;
+                }
+            }
+        }
     }
-    if (threadIdx.x == 0) { cos_sum[col] = sc[0]; sin_sum[col] = ss[0]; }
+#pragma unroll
+    for (int k = 0; k < REDUCE_CPT; ++k) {
+        const int col = blockIdx.x * REDUCE_COLS + k * REDUCE_THREADS + threadIdx.x;
+        if (col < n_cols && w1 > w0) {
+            atomicAdd(&accum[col], (unsigned long long)__double2ll_rn(cs[k] * 4294967296.0));
+            atomicAdd(&accum[n_cols + col], (unsigned long long)__double2ll_rn(sn[k] * 4294967296.0));
+        }
+    }
+}
+
+__global__ void reduce_Y_finish_kernel(const long long* accum, int n_cols, double* cos_sum, double* sin_sum) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= n_cols) return;
+    cos_sum[col] = (double)accum[col] * 0x1p-32;
+    sin_sum[col] = (double)accum[n_cols + col] * 0x1p-32;
 }
 
 }  // namespace madi
@@ -894,17 +936,55 @@ extern "C" madi_status madi_walk(const madi_walk_desc* d, void* stream) {
     return per ? launch_np<MADI_OUT_Y, true>(d, s) : launch_np<MADI_OUT_Y, false>(d, s);
 }
 
+extern "C" int64_t madi_reduce_Y_scratch_bytes(int32_t n_cols) {
+    return n_cols > 0 ? 16ll * n_cols : 0;
+}
+
 extern "C" madi_status madi_reduce_Y(const double* Y, int64_t n_walkers, int32_t n_grid, const int32_t* jd,
                                      const int32_t* jD, const int32_t* js, const double* coef, int32_t n_cols,
-                                     double* cos_sum, double* sin_sum, void* stream) {
+                                     double* cos_sum, double* sin_sum, void* scratch, int64_t scratch_bytes,
+                                     void* stream) {
     host::clear_error();
-    if (!Y || !jd || !jD || !js || !coef || !cos_sum || !sin_sum || n_walkers < 0 || n_grid <= 0 || n_cols < 0)
+    if (!Y || !jd || !jD || !js || !coef || !cos_sum || !sin_sum || n_walkers < 0 || n_grid <= 0 ||
+        n_grid > MADI_MAX_GRID || n_cols < 0)
         return host::fail(MADI_ERR_INVALID, "bad reduce_Y arguments");
     if (n_cols == 0) return MADI_OK;
-    reduce_Y_kernel<<<n_cols, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(Y, n_walkers, n_grid, jd, jD, js,
-                                                                               coef, cos_sum, sin_sum);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return host::cuda_fail(e, "reduce_Y launch");
+    if (!scratch || scratch_bytes < madi_reduce_Y_scratch_bytes(n_cols))
+        return host::fail(MADI_ERR_CAPACITY, "reduce_Y: scratch %lld < %lld bytes", (long long)scratch_bytes,
+                          (long long)madi_reduce_Y_scratch_bytes(n_cols));
+    if ((reinterpret_cast<uintptr_t>(scratch) & 7) != 0) return host::fail(MADI_ERR_INVALID, "reduce_Y: scratch must be 8-byte aligned");
+    // the fixed-point column totals hold 3 n_walkers 2^32 < 2^63
+    if (n_walkers > 500000000ll) return host::fail(MADI_ERR_UNSUPPORTED, "reduce_Y: at most 5e8 walkers");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned long long* accum = static_cast<unsigned long long*>(scratch);
+    cudaError_t e = cudaMemsetAsync(accum, 0, (size_t)madi_reduce_Y_scratch_bytes(n_cols), s);
+    if (e != cudaSuccess) return host::cuda_fail(e, "reduce_Y memset");
+    if (n_walkers > 0) {
+        // walker rows staged per round: up to 96 KB of shared memory
+        const int row_bytes = n_grid * 3 * 8;
+        const int wt = std::max(1, std::min(32, (96 * 1024) / row_bytes));
+        const size_t smem = (size_t)wt * row_bytes;
+        e = cudaFuncSetAttribute(reduce_Y_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return host::cuda_fail(e, "reduce_Y attribute");
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int gx = (n_cols + REDUCE_COLS - 1) / REDUCE_COLS;
+        // about 4 CTAs per SM over all column blocks, each walker range a multiple of wt
+        const int64_t want = std::max<int64_t>(1, (4ll * sms + gx - 1) / gx);
+        int64_t per = (n_walkers + want - 1) / want;
+        per = std::max<int64_t>(wt, (per + wt - 1) / wt * wt);
+        const int64_t gy = (n_walkers + per - 1) / per;
+        if (gy > 65535) return host::fail(MADI_ERR_UNSUPPORTED, "reduce_Y: too many walker blocks");
+        reduce_Y_kernel<<<dim3((unsigned)gx, (unsigned)gy), REDUCE_THREADS, smem, s>>>(Y, n_walkers, n_grid, wt, per, jd, jD,
+                                                                                       js, coef, n_cols, accum);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return host::cuda_fail(e, "reduce_Y launch");
+    }
+    reduce_Y_finish_kernel<<<(n_cols + 255) / 256, 256, 0, s>>>(reinterpret_cast<const long long*>(accum), n_cols,
+                                                                cos_sum, sin_sum);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return host::cuda_fail(e, "reduce_Y finish");
     return MADI_OK;
 }
 

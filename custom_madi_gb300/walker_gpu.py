@@ -553,10 +553,7 @@ def simulate_jobs(jobs: Sequence[WalkJob], cfg: SimConfig, columns: Tuple, *, di
             batch.launch()
             cs = torch.empty(len(pc), dtype=torch.float64, device=batch.dev)
             ss = torch.empty_like(cs)
-            st = N.lib().madi_reduce_Y(N.ptr(batch.Y), batch.n_rows, cfg.n_grid, N.ptr(jd), N.ptr(jD), N.ptr(js),
-                                       N.ptr(pc), len(pc), N.ptr(cs), N.ptr(ss),
-                                       torch.cuda.current_stream(batch.dev).cuda_stream)
-            N.check(st, "madi_reduce_Y")
+            N.reduce_Y(batch.Y, batch.n_rows, cfg.n_grid, jd, jD, js, pc, cs, ss, torch.cuda.current_stream(batch.dev))
             r = batch.results()[0]
             r["cos"] = cs.cpu().numpy()[:, None]
             r["sin"] = ss.cpu().numpy()[:, None]

@@ -237,11 +237,17 @@ madi_status madi_walk_batched(const madi_walk_desc* desc, void* stream);
 
 /* Replaces _reduce_kernel (madi/walker_gpu.py:658-695) for grids too large for
  * the fused epilogue: Y [n_walkers][n_grid][3] fp64 -> cos_sum / sin_sum
- * [n_cols] fp64 over the 3 axes, columns (jd, jD, js, coef). */
-madi_status madi_reduce_Y(const double* Y, int64_t n_walkers, int32_t n_grid,
-                          const int32_t* jd, const int32_t* jD, const int32_t* js,
-                          const double* coef, int32_t n_cols,
-                          double* cos_sum, double* sin_sum, void* stream);
+ * [n_cols] fp64, the sums over walkers and the 3 axes of cos / sin(coef dM),
+ * dM = Y[jd] + Y[jD] - Y[js] per column (jd, jD, js, coef).  Y is read once per
+ * block of 1,024 columns; per-CTA fp64 partials are added as 2^-32 fixed-point
+ * integers, so the result is independent of scheduling (each partial rounded
+ * once: |error| <= 2^-33 per walker block and column).  scratch: device,
+ * 8-byte aligned, madi_reduce_Y_scratch_bytes(n_cols) bytes, no initialisation
+ * needed. */
+int64_t madi_reduce_Y_scratch_bytes(int32_t n_cols);
+madi_status madi_reduce_Y(const double* Y, int64_t n_walkers, int32_t n_grid, const int32_t* jd,
+                          const int32_t* jD, const int32_t* js, const double* coef, int32_t n_cols,
+                          double* cos_sum, double* sin_sum, void* scratch, int64_t scratch_bytes, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Library match                                                            */

@@ -184,9 +184,7 @@ def test_reduce_Y_matches_oracle_reduction_on_a_large_column_grid():
     pc = torch.from_numpy(np.asarray(c[3], np.float64)).to(dev)
     cs = torch.empty(len(pc), dtype=torch.float64, device=dev)
     ss = torch.empty_like(cs)
-    st = N.lib().madi_reduce_Y(N.ptr(b.Y), n, cfg.n_grid, N.ptr(jd), N.ptr(jD), N.ptr(js), N.ptr(pc), len(pc),
-                               N.ptr(cs), N.ptr(ss), torch.cuda.current_stream(dev).cuda_stream)
-    N.check(st, "madi_reduce_Y")
+    N.reduce_Y(b.Y, n, cfg.n_grid, jd, jD, js, pc, cs, ss, torch.cuda.current_stream(dev))
     Y = b.Y.cpu().numpy()
     oc, os_ = O.reduce(Y, *c)
     np.testing.assert_allclose(cs.cpu().numpy(), oc, rtol=1e-9, atol=1e-9 * 3 * n)
@@ -306,3 +304,35 @@ def test_walk_batched_abi_equals_walk():
     got = [r["cos_fixed"] for r in b.results()]
     for a, g in zip(want, got):
         np.testing.assert_array_equal(a, g)
+
+
+def test_reduce_Y_at_the_production_column_grid():
+    """The reference's default (delta, Delta, b) grid: 1,245 pairs x 25 b =
+    31,125 columns at T = 128 ms.  A walked Y of 1,024 walkers reduced on the GPU
+    equals the oracle's fp64 reduction to 1e-9, bit-identically run to run."""
+    import torch
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300.ensemble import create_ensemble
+    from custom_madi_gb300.walker_gpu import WalkBatch, WalkJob
+    from oracle import oracle as O
+    n = 1024
+    cfg = SimConfig(boundary_mode="periodic", n_cells=64, n_walkers=n, n_ensembles=1, ts=0.01,
+                    geometry_validation_points=20_000, geometry_vi_tolerance=0.1)
+    cols, c = _columns(cfg)
+    assert len(c[3]) == 31_125 and cfg.n_grid == 129
+    ens = create_ensemble(2.0e5, 4.0, cfg, seed=8)
+    b = WalkBatch([WalkJob(ens, 0.02, 17, n)], cfg, out_mode=N.MADI_OUT_Y)
+    b.launch()
+    dev = b.dev
+    jd, jD, js = (torch.from_numpy(np.asarray(x, np.int32)).to(dev) for x in c[:3])
+    pc = torch.from_numpy(np.asarray(c[3], np.float64)).to(dev)
+    outs = []
+    for _ in range(2):
+        cs = torch.empty(len(pc), dtype=torch.float64, device=dev)
+        ss = torch.empty_like(cs)
+        N.reduce_Y(b.Y, n, cfg.n_grid, jd, jD, js, pc, cs, ss, torch.cuda.current_stream(dev))
+        outs.append((cs.cpu().numpy(), ss.cpu().numpy()))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    oc, os_ = O.reduce(b.Y.cpu().numpy(), *c)
+    np.testing.assert_allclose(outs[0][0], oc, rtol=1e-9, atol=1e-9 * 3 * n)
+    np.testing.assert_allclose(outs[0][1], os_, rtol=1e-9, atol=1e-9 * 3 * n)
