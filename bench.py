@@ -244,6 +244,7 @@ def main(argv=None):
     from custom_madi_gb300 import signal as S
     from custom_madi_gb300.walker_gpu import LaunchConfig, WalkBatch, WalkGraph, pair_layout
     from custom_madi_gb300 import autotune
+    from custom_madi_gb300.sharding import max_over_ranks
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -287,11 +288,7 @@ def main(argv=None):
         dist.barrier()
     dev_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     steps_per_run = sum(j.n_walkers for j in jobs) * cfg.n_steps
-    t_max = dev_s
-    if ws > 1:
-        t = torch.tensor([dev_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(dev_s)             # the slowest rank sets the job's time
     value = ws * steps_per_run * args.steps / t_max
     batched_results = batch.results()
     # ---- end to end: host geometry + job tables -> device -> walk -> host sums ----
@@ -301,7 +298,7 @@ def main(argv=None):
         t0 = time.perf_counter()
         batch.run_from_host(host)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = float(np.mean(e2e_t[1:])) if len(e2e_t) > 1 else float("nan")
+    e2e_s = max_over_ranks(float(np.mean(e2e_t[1:])) if len(e2e_t) > 1 else float("nan"))
     e2e_val = steps_per_run / e2e_s * ws
     # ---- roofline (issue bound: lane-operations per walker-step) ----
     n_ws = max(int(counters[0]) * cfg.n_steps, 1)
@@ -604,7 +601,9 @@ def mixed_leg(dev, lib, threads):
         for i, n in enumerate(sizes):
             reqs.append(FitRequest(vox[:n], "bf16", 32, arrival=0.5 * (i + 1)))
         n_fit = len(sizes)
-    srv = Server(cfg, lay, dirs, library=lib, device=dev, n_slots=len(ens), budget_bytes=32 << 30)
+    # 1e6-walker entries: launches of four waves (~622k walkers) amortise each launch's tail
+    srv = Server(cfg, lay, dirs, library=lib, device=dev, n_slots=len(ens), budget_bytes=32 << 30,
+                 chunk_walkers=262_144, launch_walkers=622_592)
     out = srv.run(reqs, realtime=True)
     sims = [r for r in out["records"] if r.kind == "sim"]
     fits = [r for r in out["records"] if r.kind == "fit"]
