@@ -6,11 +6,11 @@
 // tile are converted to BF16 in shared memory (K = features padded to 32,
 // K-major, no-swizzle UMMA layout); the library, pre-packed once into 8 KB
 // tiles of 128 entries in the same layout, streams through four shared stages
-// by cp.async.bulk.  Lane 0 of the producer warp issues tcgen05.mma (M=128,
-// N=128, K=16, two per tile) into one of four 128-column FP32 TMEM
-// accumulators.  Two epilogue warpgroups split each tile's columns: every
-// thread owns one voxel row (its TMEM lane) and keeps a top-k of that row over
-// its half of the library.
+// by cp.async.bulk, two tiles per step.  Lane 0 of the producer warp issues
+// tcgen05.mma (M=128, N=256 = the step's two tiles, K=16, two per step) into
+// one of two 256-column FP32 TMEM accumulators.  Epilogue warpgroup h takes
+// tile h of every step: every thread owns one voxel row (its TMEM lane) and
+// keeps a top-k of that row over its half of the library.
 //
 // Scores (smaller is better):
 //   fixed S0: score_j = |L~_j|^2 - 2 m~.L~_j  (= |m~ - L~_j|^2 - |m~|^2)
@@ -21,8 +21,9 @@
 // 1 in A and a three-term BF16 split of -|L~_j|^2 / 2 in B, so the accumulator
 // is t_j = m~.L~_j - |L~_j|^2 / 2 = -score_j / 2 to fp32 accuracy.
 //
-// Epilogue per 32-column chunk: the row's 32 keys are staged in shared memory,
-// a 32-bit mask marks those under the row's current k-th best, and only the
+// Epilogue per 64-column pass: a warp-uniform test skips passes where no row of
+// the warp can hold a candidate; otherwise the keys are staged in shared
+// memory, bit masks mark those under the row's current k-th best, and only the
 // marked ones are appended to the row's candidate buffer.  When any lane's
 // buffer would overflow, the warp folds all buffers into the sorted register
 // top-k with bitonic networks.  Each warpgroup rescores its k candidates in
@@ -602,9 +603,10 @@ MADI_DEV void append_pass(uint32_t& ma, int oa, uint32_t& mb, int ob, float2*& w
 }
 
 // ---------------------------------------------------------------------------
-// Main kernel: warps 0-7 are the epilogue (warpgroup h = warp / 4 takes
-// columns [64h, 64h + 64) of every tile; thread tid % 128 = voxel row = TMEM
-// lane), lane 0 of warp 8 is the producer (library loads and MMA issue).
+// Main kernel: warps 0-7 are the epilogue (warpgroup h = warp / 4 takes tile
+// h of every step, accumulator columns [128h, 128h + 128), in two 64-column
+// passes; thread tid % 128 = voxel row = TMEM lane), lane 0 of warp 8 is the
+// producer (library loads and MMA issue).
 // Hand-offs use mbarriers only (every wait bounded):
 //   full[s]             : library stage s loaded (a stage is refilled only once
 //                         the acce wait has certified its MMA complete)
