@@ -233,6 +233,7 @@ def main(argv=None):
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop legs")
     ap.add_argument("--no-mixed", action="store_true", help="skip the large mixed workload")
     ap.add_argument("--no-match", action="store_true", help="skip the library-match leg")
+    ap.add_argument("--no-refdesign", action="store_true", help="skip the reference-design plain leg")
     ap.add_argument("--serving-requests", type=int, default=200)
     args = ap.parse_args(argv)
     ws, rank, local = _dist()
@@ -353,6 +354,9 @@ def main(argv=None):
         sec["plain_vs_batched"] = plain_and_served(dev, cfg, jobs, lay, dirs, value, batch)
         del batch
         torch.cuda.empty_cache()
+        if not args.no_refdesign:
+            sec["reference_design_plain"] = reference_design_leg(dev, cfg, jobs, cols, value)
+        torch.cuda.empty_cache()
         lib = None
         if not args.no_match:
             sec["match"], lib = match_leg(dev, threads)
@@ -442,6 +446,48 @@ def plain_and_served(dev, cfg, jobs, lay, dirs, batched_rate, batch):
                 "note": "matched Monte Carlo error: every arm walks the same 1e5 walkers per entry; "
                         "sums are exact fixed point, so the arms are compared bit for bit"})
     return out
+
+
+def reference_design_leg(dev, cfg, jobs, cols, batched_rate, n_entries=4):
+    """The reference's GPU design for the same entries (madi/walker_gpu.py:
+    520-695 kernels, :989-1063 launch): per entry the geometry H2D, one fp64
+    walk launch (one thread per walker, exact KD rule every step, Y stored to
+    HBM), the column reduction over the 3 axes, synchronize, D2H of the sums.
+    Both kernels are this package's CUDA; the entries, walkers and Philox
+    numbers are the batched arm's, so the Monte Carlo error is matched."""
+    import torch
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300.walker_gpu import WalkBatch
+    sub = jobs[:n_entries]
+    host = [_host_geometry(j.ensemble, dev) for j in sub]
+    st = torch.cuda.current_stream(dev)
+    jd, jD, js = (torch.from_numpy(np.asarray(a, np.int32)).to(dev) for a in (cols.j_delta, cols.j_Delta, cols.j_sum))
+    pc = torch.from_numpy(np.asarray(cols.phase_coef, np.float64)).to(dev)
+    cs = torch.empty(len(pc), dtype=torch.float64, device=dev)
+    ss = torch.empty_like(cs)
+
+    def one(j, hg):
+        for d, h in hg:
+            d.copy_(h, non_blocking=True)
+        b = WalkBatch([j], cfg, out_mode=N.MADI_OUT_Y, precision=64, device=dev)
+        b.launch()
+        N.reduce_Y(b.Y, b.n_rows, cfg.n_grid, jd, jD, js, pc, cs, ss, st)
+        r = b.results()[0]
+        return cs.cpu().numpy(), r["counters"]
+
+    one(sub[0], host[0])                            # warm-up
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    sums = [one(j, hg) for j, hg in zip(sub, host)]
+    t = time.perf_counter() - t0
+    steps = sum(j.n_walkers for j in sub) * cfg.n_steps
+    rate = steps / t
+    ok = all(c["escaped"] == 0 and c["classifier_error"] == 0 for _, c in sums)
+    return {"entries": len(sub), "walkers_per_entry": int(sub[0].n_walkers), "s": t,
+            "walker_steps_per_s": rate, "batched_over_reference_design": batched_rate / rate,
+            "clean": bool(ok),
+            "note": "the reference's GPU design (fp64, one thread per walker, exact KD rule every step, "
+                    "Y stored, separate reduction), one entry per launch, as CUDA kernels of this package"}
 
 
 def match_leg(dev, threads):

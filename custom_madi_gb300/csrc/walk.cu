@@ -640,10 +640,37 @@ __global__ void __launch_bounds__(256, MINB) walk_f32_kernel(const madi_walk_des
 }
 
 // ---------------------------------------------------------------------------
-// fp64 replay of a fixed random stream (golden check; madi/walker_gpu.py:698-840
-// arithmetic: separately rounded fp64, reference origin L/2, exact KD rule).
-// One thread per walker of jobs[0].
+// fp64 walker (madi/walker_gpu.py:520-585 design and :698-840 arithmetic:
+// separately rounded fp64, reference origin L/2, exact KD rule at every step,
+// Y stored).  One thread per walker of jobs[0]; it replays a fixed random
+// stream (golden check) or walks the fp32 walker's Philox numbers.
 // ---------------------------------------------------------------------------
+// Normals of step `step` of walker widx from the Philox stream of the fp32
+// walker, in fp64 (Box-Muller: u1 = (w + 1/2) 2^-32, u2 = (w' >> 8) 2^-24), and
+// the step's acceptance word: the fp32 walker's random numbers, evaluated in
+// the reference's precision.
+MADI_DEV void normals_f64(uint32_t widx, int step, uint32_t k0, uint32_t k1, double (&n)[3], uint32_t& word) {
+    const uint32_t pair = (uint32_t)step >> 1;
+    const U4 ra = philox10(U4{widx, pair, 0u, 0u}, k0, k1);
+    const U4 rb = philox10(U4{widx, pair, 1u, 0u}, k0, k1);
+    const uint32_t wd[6] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y};
+    double gv[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double u1 = __dadd_rn(__dmul_rn((double)wd[2 * k], 2.3283064365386963e-10), 1.1641532182693481e-10);
+        const double u2 = __dmul_rn((double)(wd[2 * k + 1] >> 8), 5.9604644775390625e-08);
+        const double r = sqrt(__dmul_rn(-2.0, log(u1)));
+        double sn, cs;
+        sincos(__dmul_rn(6.283185307179586, u2), &sn, &cs);
+        gv[2 * k] = __dmul_rn(r, cs);
+        gv[2 * k + 1] = __dmul_rn(r, sn);
+    }
+    const bool odd = (step & 1) != 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) n[k] = odd ? gv[3 + k] : gv[k];
+    word = (step & 1) ? rb.w : rb.z;
+}
+
 __global__ void __launch_bounds__(128) walk_f64_kernel(const madi_walk_desc d) {
     const madi_walk_job job = d.jobs[0];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
@@ -652,9 +679,25 @@ __global__ void __launch_bounds__(128) walk_f64_kernel(const madi_walk_desc d) {
     const Geo g = make_geo(gd, reinterpret_cast<const unsigned char*>(gd.stage));
     const bool periodic = gd.boundary == MADI_BOUNDARY_PERIODIC;
     const bool cells = gd.has_cells != 0;
+    const bool stream = d.rng == MADI_RNG_STREAM;
+    const uint32_t widx = job.walker_base + (uint32_t)w;
     const double L = gd.L, half_L = gd.L / 2.0, ts = d.ts, pp = job.pp;
     const size_t row = (size_t)job.y_row + w;
-    double px = d.init[3 * (size_t)w], py = d.init[3 * (size_t)w + 1], pz = d.init[3 * (size_t)w + 2];
+    double px, py, pz;
+    if (stream) {
+        px = d.init[3 * (size_t)w]; py = d.init[3 * (size_t)w + 1]; pz = d.init[3 * (size_t)w + 2];
+    } else {
+        const U4 r = philox10(U4{widx, 0u, 0u, 1u}, job.key0, job.key1);
+        const double span = gd.source_hi - gd.source_lo;
+        px = gd.source_lo + span * ((double)r.x * 2.3283064365386963e-10);
+        py = gd.source_lo + span * ((double)r.y * 2.3283064365386963e-10);
+        pz = gd.source_lo + span * ((double)r.z * 2.3283064365386963e-10);
+        if (periodic) {
+            if (px >= L) px = 0.0;
+            if (py >= L) py = 0.0;
+            if (pz >= L) pz = 0.0;
+        }
+    }
     int cell = 0, inside = 0, escaped = 0, cerr = 0;
     uint32_t n_acc = 0, n_rej = 0, n_full = 0;
     if (cells) {
@@ -672,10 +715,17 @@ __global__ void __launch_bounds__(128) walk_f64_kernel(const madi_walk_desc d) {
     It[0] = (int8_t)inside;
     for (int step = 0; step < d.n_steps; ++step) {
         if (!escaped && !cerr) {
-            const size_t o = (size_t)step * job.n_walkers + w;
-            double qx = __dadd_rn(px, d.incr[3 * o]), qy = __dadd_rn(py, d.incr[3 * o + 1]),
-                   qz = __dadd_rn(pz, d.incr[3 * o + 2]);
-            const double u = d.unif[o];
+            double inc[3], u = 0.0;
+            uint32_t word = 0;
+            if (stream) {
+                const size_t o = (size_t)step * job.n_walkers + w;
+                inc[0] = d.incr[3 * o]; inc[1] = d.incr[3 * o + 1]; inc[2] = d.incr[3 * o + 2];
+                u = d.unif[o];
+            } else {
+                normals_f64(widx, step, job.key0, job.key1, inc, word);
+                inc[0] = __dmul_rn(inc[0], d.sigma); inc[1] = __dmul_rn(inc[1], d.sigma); inc[2] = __dmul_rn(inc[2], d.sigma);
+            }
+            double qx = __dadd_rn(px, inc[0]), qy = __dadd_rn(py, inc[1]), qz = __dadd_rn(pz, inc[2]);
             int qkx = kx, qky = ky, qkz = kz;
             bool ok = true;
             if (periodic) {
@@ -704,8 +754,19 @@ __global__ void __launch_bounds__(128) walk_f64_kernel(const madi_walk_desc d) {
                     else if (inside && nin && cell != ncell) m = 2;
                     bool accept = true;
                     if (m > 0 && pp < 1.0) {
-                        const double thr = m == 1 ? pp : __dmul_rn(pp, pp);
-                        accept = !(u >= thr);
+                        if (stream) {
+                            const double thr = m == 1 ? pp : __dmul_rn(pp, pp);
+                            accept = !(u >= thr);
+                        } else {            // 64-bit uniform against floor(pp^m 2^64), as the fp32 walker
+                            const uint64_t thr = m == 1 ? job.thr1 : job.thr2;
+                            const uint32_t th = (uint32_t)(thr >> 32);
+                            if (word != th) {
+                                accept = word < th;
+                            } else {
+                                const U4 rc = philox10(U4{widx, (uint32_t)step, 2u, 0u}, job.key0, job.key1);
+                                accept = rc.x < (uint32_t)thr;
+                            }
+                        }
                         if (accept) ++n_acc; else ++n_rej;
                     }
                     if (accept) {
@@ -898,9 +959,8 @@ extern "C" madi_status madi_walk(const madi_walk_desc* d, void* stream) {
         return host::fail(MADI_ERR_INVALID, "stream replay needs init / incr / unif");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (d->precision == 64) {
-        if (d->rng != MADI_RNG_STREAM) return host::fail(MADI_ERR_UNSUPPORTED, "fp64 walker replays streams only");
-        if (d->n_jobs != 1) return host::fail(MADI_ERR_UNSUPPORTED, "fp64 replay walks one job");
-        if (!d->Y || !d->inside_trace) return host::fail(MADI_ERR_INVALID, "fp64 replay writes Y and inside_trace");
+        if (d->n_jobs != 1) return host::fail(MADI_ERR_UNSUPPORTED, "fp64 walker walks one job");
+        if (!d->Y || !d->inside_trace) return host::fail(MADI_ERR_INVALID, "fp64 walker writes Y and inside_trace");
         // The job is read on the device; the host only needs its walker count, passed as n_tiles * 128 bound.
         const int blocks = d->n_tiles;
         walk_f64_kernel<<<blocks, 128, 0, s>>>(*d);

@@ -458,7 +458,8 @@ def run_walk_Y(ens: Ensemble, kio: float, cfg: Optional[SimConfig] = None, seed:
 
     A replay stream runs the fp64 walker (reference arithmetic, exact KD rule)
     unless precision=32 asks for the production fp32 walker; without a stream
-    the fp32 walker draws Philox4x32-10 numbers keyed by ``seed``.
+    the walker draws Philox4x32-10 numbers keyed by ``seed`` (fp32 walker by
+    default; precision=64 walks the same numbers with the fp64 walker).
     """
     _require_gpu(use_gpu)
     if cfg is None:
@@ -469,8 +470,6 @@ def run_walk_Y(ens: Ensemble, kio: float, cfg: Optional[SimConfig] = None, seed:
     if random_stream is not None:
         random_stream.validate(cfg, ens)
     prec = precision or (64 if random_stream is not None else 32)
-    if prec == 64 and random_stream is None:
-        raise ValueError("the fp64 walker replays a fixed random stream only")
     batch = WalkBatch([WalkJob(ens, actual_pp, int(seed), int(cfg.n_walkers))], cfg, out_mode=N.MADI_OUT_Y,
                       stream=random_stream, precision=prec, launch=launch)
     batch.launch()
@@ -531,12 +530,19 @@ class WalkGraph:
 
 
 def simulate_jobs(jobs: Sequence[WalkJob], cfg: SimConfig, columns: Tuple, *, dirs=None,
-                  launch: Optional[LaunchConfig] = None, check: bool = True) -> list:
-    """Walk every job in one persistent launch; per job cos / sin sums [n_cols, n_dirs]."""
+                  launch: Optional[LaunchConfig] = None, check: bool = True, precision: int = 32) -> list:
+    """Walk every job in one persistent launch; per job cos / sin sums [n_cols, n_dirs].
+
+    precision=64 runs the reference's GPU design instead (madi/walker_gpu.py:
+    520-695, :989-1063): per job one fp64 walk launch that stores Y, then a
+    column reduction over the 3 Cartesian axes (sums [n_cols, 1]).
+    """
     _require_gpu(None)
+    if precision not in (32, 64):
+        raise ValueError("precision must be 32 or 64")
     layout = pair_layout(*columns)
     u = cfg.direction_array() if dirs is None else np.asarray(dirs, np.float64)
-    if fused_supported(layout, len(u)):
+    if precision == 32 and fused_supported(layout, len(u)):
         batch = WalkBatch(jobs, cfg, layout=layout, dirs=u, launch=launch)
         batch.launch()
         torch.cuda.current_stream(batch.dev).synchronize()
@@ -549,7 +555,7 @@ def simulate_jobs(jobs: Sequence[WalkJob], cfg: SimConfig, columns: Tuple, *, di
             np.asarray(columns[0], np.int32), np.asarray(columns[1], np.int32), np.asarray(columns[2], np.int32),
             np.asarray(columns[3], np.float64)))
         for j in jobs:
-            batch = WalkBatch([j], cfg, out_mode=N.MADI_OUT_Y, launch=launch)
+            batch = WalkBatch([j], cfg, out_mode=N.MADI_OUT_Y, launch=launch, precision=precision)
             batch.launch()
             cs = torch.empty(len(pc), dtype=torch.float64, device=batch.dev)
             ss = torch.empty_like(cs)

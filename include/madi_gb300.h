@@ -168,6 +168,11 @@ enum {
  *
  * rng MADI_RNG_STREAM replays init[w][3], incr[step][w][3], unif[step][w]
  * (WalkRandomStream, madi/walker_gpu.py:86-127), fp64 arrays.
+ *
+ * precision 64 is the reference's walker design (madi/walker_gpu.py:520-585):
+ * one thread per walker of jobs[0], separately rounded fp64 arithmetic, the
+ * exact KD rule at every step, Y output only; n_tiles = ceil(n_walkers / 128).
+ * With MADI_RNG_PHILOX it evaluates the fp32 walker's Philox numbers in fp64.
  */
 typedef struct madi_walk_desc {
     const madi_geometry* geoms;    /* device array                                    */
@@ -178,7 +183,7 @@ typedef struct madi_walk_desc {
     int32_t grid_blocks;           /* persistent CTAs; 0 = one per tile               */
     int32_t stage_smem;            /* max stage_bytes over geoms; 0 = read in place   */
     int32_t boundary;              /* MADI_BOUNDARY_* shared by every geometry        */
-    int32_t precision;             /* 32 = fp32 production walker, 64 = fp64 replay   */
+    int32_t precision;             /* 32 = fp32 production walker, 64 = fp64 walker   */
     int32_t rng;                   /* MADI_RNG_*                                      */
     int32_t out_mode;              /* MADI_OUT_*                                      */
     int32_t n_steps, steps_per_h, n_grid;

@@ -316,3 +316,53 @@ def test_philox_si_walk_tracks_oracle_same_key(golden):
     assert np.mean(same) >= 0.95, np.mean(same)
     assert np.mean(tel["inside_trace"][same] == o["inside_trace"][same]) >= 0.999
     assert 0.2 < float(np.mean(tel["inside_trace"])) < 0.95
+
+
+def test_fp64_philox_walk_matches_oracle_same_key(golden):
+    """The fp64 walker on Philox numbers (the reference's walker design:
+    one thread per walker, exact KD rule every step, Y stored) against the
+    fp64 oracle on the same key, finite SI box with fatal escape.  Both evaluate
+    the same separately rounded fp64 arithmetic; log / sin / cos may differ by
+    an ulp between CUDA and the C library, so Y agrees to 1e-9 um ms and the
+    labels exactly for (nearly) every walker."""
+    from custom_madi_gb300.ensemble import ensemble_from_arrays
+    from custom_madi_gb300.walker_gpu import PHILOX_KEY1, run_walk_Y
+    from oracle import oracle as O
+    d = golden("classify_si.npz")
+    ens = ensemble_from_arrays(d["seeds"], d["annulus"], float(d["L"]), source_lo=float(d["source_lo"]),
+                               source_hi=float(d["source_hi"]), rho_per_uL=float(d["rho"]))
+    n, steps = 512, 400
+    cfg = SimConfig(L=float(d["L"]), n_walkers=n, n_ensembles=1, ts=0.01, T_max_ms=4.0, h_ms=0.01,
+                    small_deltas=[0.01], big_deltas=[0.01], b_values=[0.0])
+    Y, _, tel = run_walk_Y(ens, 0.0, cfg, seed=4321, pp=0.05, return_telemetry=True, precision=64, verbose=False)
+    o = O.walk(O.geom_arrays(ens), n_walkers=n, n_steps=steps, steps_per_h=1, n_grid=steps + 1, sigma=cfg.sigma,
+               ts=cfg.ts, pp=0.05, key=(4321, PHILOX_KEY1))
+    same = np.all(np.abs(Y - o["Y"]) <= 1e-9, axis=(1, 2))
+    assert np.mean(same) >= 0.998, np.mean(same)
+    assert np.array_equal(tel["inside_trace"][same], o["inside_trace"][same])
+    assert 0.2 < float(np.mean(tel["inside_trace"])) < 0.95
+    print("fp64 Philox max |dY| over matching walkers =", float(np.abs(Y - o["Y"])[same].max()))
+
+
+def test_reference_design_path_matches_oracle_signal():
+    """simulate_jobs(precision=64): per-entry fp64 walk storing Y, then the tiled
+    column reduction, on a periodic 64-cell box; the signal sums agree with the
+    oracle's fp64 walk on the same key to 1e-9 of the walker count."""
+    from custom_madi_gb300 import signal as S
+    from custom_madi_gb300.walker_gpu import PHILOX_KEY1, WalkJob, kio_to_pp, pair_layout, simulate_jobs
+    cfg, ens = _periodic_c0(1000)
+    cols = S.build_columns(cfg)
+    pp = kio_to_pp(20.0, ens.mean_AV, cfg)
+    r = simulate_jobs([WalkJob(ens, pp, 555, 1000)], cfg, (cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef),
+                      dirs=np.eye(3), precision=64)[0]
+    cs, out = _oracle_sums(ens, cfg, cols, pp, (555, PHILOX_KEY1), 1000, dirs=np.eye(3))
+    lay = pair_layout(cols.j_delta, cols.j_Delta, cols.j_sum, cols.phase_coef)
+    want = np.full(len(cols.phase_coef), np.nan)
+    for p in range(lay.n_pairs):                 # oracle sums are per (pair, b) of the layout
+        for b in range(lay.n_b):
+            if lay.col_of[p, b] >= 0:
+                want[lay.col_of[p, b]] = cs[p * lay.n_b + b].sum()
+    got = r["cos"][:, 0]
+    assert not np.isnan(want).any()
+    assert np.max(np.abs(got - want)) <= 1e-9 * 1000, np.max(np.abs(got - want))
+    assert np.array_equal(r["occupancy"], out["occupancy"])
