@@ -37,6 +37,7 @@ MADI_MATCH_FREE_S0 = 1
 MADI_MATCH_FP32 = 0
 MADI_MATCH_BF16 = 1
 MADI_MATCH_FLAG_TEST_STALL = 1
+MADI_MATCH_FLAG_FULL_SCAN = 2
 
 CNT_NAMES = ("walkers", "escaped", "classifier_error", "full", "tier1", "fallback64",
              "cross_accept", "cross_reject", "facet_pass")

@@ -65,6 +65,7 @@ constexpr uint32_t STALL_POLLS = 64;            // the test-only stalled wait (M
 // Status word in the scratch, read by madi_match_wait: 0 ok, 1 a bounded wait
 // ran out (every issued copy and MMA then drained), 2 the drain ran out too.
 constexpr int ERR_TIMEOUT = 1;
+constexpr float U_BF16 = 0.00390625f;           // BF16 round-to-nearest: |bf16(x) - x| <= 2^-8 |x|
 constexpr int ERR_DRAIN = 2;
 
 enum { MODE_FOLD = 0, MODE_AUX = 1, MODE_FREE = 2 };
@@ -204,7 +205,7 @@ __global__ void column_mean_kernel(const float* lib, int n_lib, int F, float* mu
 // Also copies the fp32 row into lrows[e][0..KPAD) (zero padded, 128-byte rows)
 // for the rescore.
 __global__ void pack_library_kernel(const float* lib, int n_lib, int F, int n_tiles, int mode, const float* mu,
-                                    const int32_t* lperm, unsigned char* tiles, float* aux, float* lrows) {
+                                    const int32_t* lperm, unsigned char* tiles, float* aux, float* lrows, float* lmax) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (int64_t)n_tiles * TILE_N) return;
     const int t = (int)(e / TILE_N), n = (int)(e % TILE_N);
@@ -212,12 +213,14 @@ __global__ void pack_library_kernel(const float* lib, int n_lib, int F, int n_ti
     const bool live = e < n_lib;
     const int64_t src = live ? lperm[e] : 0;
     double q = 0.0;
+    float n2 = 0.f;                                // |L - mu|^2 in fp32 (the bounds' library term)
     for (int k = 0; k < KPAD; ++k) {
         float x = 0.f;
         if (live && k < F) {
             const float v = lib[src * F + k];
             x = mode == MODE_FREE ? v : v - mu[k];
         }
+        n2 = fmaf(x, x, n2);
         const __nv_bfloat16 xb = __float2bfloat16_rn(x);
         const double xr = (double)__bfloat162float(xb);
         q += xr * xr;
@@ -240,23 +243,25 @@ __global__ void pack_library_kernel(const float* lib, int n_lib, int F, int n_ti
         *reinterpret_cast<__nv_bfloat16*>(tile + canon_off(n, F + 1)) = mid;
         *reinterpret_cast<__nv_bfloat16*>(tile + canon_off(n, F + 2)) = lo;
     }
+    // non-negative floats order as their bit patterns; rounded up by a relative 2^-20
+    if (live && mode != MODE_FREE) atomicMax(reinterpret_cast<int*>(lmax), __float_as_int(sqrtf(n2) * (1.f + 1e-6f)));
     // Padding entries carry NaN in aux: their score fails every "<" test.
     const float qf = (float)q;
     aux[e] = live ? (mode == MODE_FREE ? 1.f / fmaxf(qf, 1e-30f) : qf) : __int_as_float(0x7fc00000);
 }
 
 // ---------------------------------------------------------------------------
-// Scan order.  The library is sorted along its principal axis and each voxel
-// tile (voxels bucketed along the same axis) visits the library tiles nearest
-// its key first, so the rows' k-th best thresholds settle within a few tiles
-// and later tiles rarely hold a candidate.  The order changes no result: the
-// top-k of a row is the k smallest scores whatever the visiting order.  Keys
-// are (x - kmu).pc with x the row (free S0: the unit row), kmu the library mean
-// of such rows and pc the leading eigenvector of their covariance.
+// Scan order.  Library entries and voxels are put in the order of 256 key
+// buckets along the library's principal axis (a stable counting sort: the
+// order is deterministic), and each voxel tile visits the library tiles
+// nearest its key first, so the rows' k-th best thresholds settle within a
+// few tiles and later tiles rarely hold a candidate.  The order changes no
+// result beyond the choice among BF16 score ties at the k-th place.  Keys are
+// (x - kmu).pc with x the row (free S0: the unit row), kmu the library mean of
+// such rows and pc the leading eigenvector of their covariance.
 // ---------------------------------------------------------------------------
-constexpr int NBUCKET = 256;                    // voxel key buckets
-constexpr int SORT_MAX = 32768;                 // libraries up to this size are sorted
-constexpr int VBLK = 1024;                      // voxels per ranking block
+constexpr int NBUCKET = 256;                    // key buckets
+constexpr int VBLK = 1024;                      // rows per ranking block
 
 MADI_DEV float row_scale(const float* x, int F, bool unit) {
     if (!unit) return 1.f;
@@ -312,7 +317,11 @@ __global__ void key_axis_kernel(const float* cov, int F, float* pc) {
         for (int b = 0; b < F; ++b) w = fmaf(lane < F ? cov[lane * F + b] : 0.f, __shfl_sync(0xffffffffu, v, b), w);
         float n2 = w * w;
         for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
-        v = n2 > 0.f ? w * rsqrtf(n2) : v;
+        const float vn = n2 > 0.f ? w * rsqrtf(n2) : v;
+        float d2 = (vn - v) * (vn - v);
+        for (int o = 16; o > 0; o >>= 1) d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+        v = vn;
+        if (d2 < 1e-12f) break;                  // warp-uniform: converged to fp32 precision
     }
     if (lane < F) pc[lane] = v;
 }
@@ -327,14 +336,9 @@ __global__ void key_kernel(const float* x, int64_t n, int F, int unit, const flo
     key[i] = k;
 }
 
-// One CTA: library order by quantised key (17 bits) then index (15 bits), a
-// deterministic bitonic sort of packed words in shared memory; also the key
-// range.  n <= SORT_MAX.
-__global__ void __launch_bounds__(1024) lib_sort_kernel(const float* key, int n, int32_t* lperm, float* krange) {
-    extern __shared__ uint32_t w[];
+// Key range of the library (one CTA).
+__global__ void __launch_bounds__(1024) key_range_kernel(const float* key, int n, float* krange) {
     __shared__ float red[2][32];
-    int n2 = 1;
-    while (n2 < n) n2 <<= 1;
     float lo = 3.0e38f, hi = -3.0e38f;
     for (int i = threadIdx.x; i < n; i += blockDim.x) { lo = fminf(lo, key[i]); hi = fmaxf(hi, key[i]); }
     for (int o = 16; o > 0; o >>= 1) {
@@ -343,48 +347,39 @@ __global__ void __launch_bounds__(1024) lib_sort_kernel(const float* key, int n,
     }
     if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = lo; red[1][threadIdx.x >> 5] = hi; }
     __syncthreads();
-    lo = red[0][0]; hi = red[1][0];
-    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) { lo = fminf(lo, red[0][i]); hi = fmaxf(hi, red[1][i]); }
-    const float scale = hi > lo ? 131071.f / (hi - lo) : 0.f;
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) {
-        if (i < n) {
-            const uint32_t q = (uint32_t)fminf(fmaxf((key[i] - lo) * scale, 0.f), 131071.f);
-            w[i] = (q << 15) | (uint32_t)i;
-        } else {
-            w[i] = 0xFFFFFFFFu;
-        }
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) { lo = fminf(red[0][0], red[0][i]); hi = fmaxf(red[1][0], red[1][i]);
+                                                            red[0][0] = lo; red[1][0] = hi; }
+        krange[0] = red[0][0];
+        krange[1] = red[1][0];
     }
-    __syncthreads();
-    for (int k = 2; k <= n2; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const uint32_t x = w[i], y = w[l];
-                    const bool up = (i & k) == 0;
-                    if ((x > y) == up) { w[i] = y; w[l] = x; }
-                }
-            }
-            __syncthreads();
-        }
-    }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) lperm[i] = (int32_t)(w[i] & 0x7FFFu);
-    if (threadIdx.x == 0) { krange[0] = lo; krange[1] = hi; }
 }
 
-__global__ void iota_kernel(int32_t* p, int64_t n) {
+// Bucket of each key over the library key range (outside values clamp).
+MADI_DEV uint8_t key_bucket(float k, const float* krange) {
+    const float lo = krange[0], hi = krange[1];
+    const float u = hi > lo ? (k - lo) / (hi - lo) : 0.f;
+    return (uint8_t)fminf(fmaxf(u * NBUCKET, 0.f), (float)(NBUCKET - 1));
+}
+
+__global__ void key_bucket_kernel(const float* key, int64_t n, const float* krange, uint8_t* vb) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = (int32_t)i;
+    if (i < n) vb[i] = key_bucket(key[i], krange);
 }
 
-// Key bounds of each library tile in scan order.
+// Key bounds (min, max) of each library tile in scan order.
 __global__ void tile_bounds_kernel(const float* key, const int32_t* lperm, int n_lib, int n_tiles, float* tlo,
                                    float* thi) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_tiles) return;
-    const int a = t * TILE_N, b = min((t + 1) * TILE_N, n_lib) - 1;
-    tlo[t] = key[lperm[a]];
-    thi[t] = key[lperm[b]];
+    float lo = 3.0e38f, hi = -3.0e38f;
+    for (int e = t * TILE_N; e < min((t + 1) * TILE_N, n_lib); ++e) {
+        const float k = key[lperm[e]];
+        lo = fminf(lo, k);
+        hi = fmaxf(hi, k);
+    }
+    tlo[t] = lo;
+    thi[t] = hi;
 }
 
 // Voxel key bucket (over the library key range; outside values clamp).
@@ -397,12 +392,10 @@ __global__ void vox_bucket_kernel(const float* meas, int64_t n_vox, int F, int u
     float k = 0.f;
     for (int f = 0; f < F; ++f) k = fmaf(r[f] * sc - kmu[f], pc[f], k);
     vkey[i] = k;
-    const float lo = krange[0], hi = krange[1];
-    const float u = hi > lo ? (k - lo) / (hi - lo) : 0.f;
-    vb[i] = (uint8_t)fminf(fmaxf(u * NBUCKET, 0.f), (float)(NBUCKET - 1));
+    vb[i] = key_bucket(k, krange);
 }
 
-// Stable rank of each voxel among the earlier voxels of its block with the
+// Stable rank of each row (voxel or library entry) among the earlier rows of its block with the
 // same bucket (warp match + per-warp histograms), and per-block counts.
 __global__ void __launch_bounds__(VBLK) vox_rank_kernel(const uint8_t* vb, int64_t n_vox, uint16_t* vrank,
                                                         uint32_t* cnt) {
@@ -478,17 +471,61 @@ __global__ void vox_scatter_kernel(const uint8_t* vb, const uint16_t* vrank, con
     vperm[base[b] + offs[(size_t)b * nblk + blk] + vrank[v]] = (int32_t)v;
 }
 
+// Steps of each voxel tile (fixed S0, after the probe launch).  Every entry j
+// of library tile o has |m~ - L~_j| >= |k(m) - k(L_j)| - u (|m - mu| + |L_j - mu|)
+// (k the principal-axis key, u the BF16 unit roundoff), and for every row of
+// the voxel tile |k(m) - k(L_j)| >= d(o) - W, with d(o) the distance of the
+// tile's key range from the voxel tile's median key and W the rows' largest
+// distance from it.  A tile whose bound exceeds every row's residual bound
+// (the probe's k-th best over the first step, plus u |m - mu|, plus u max|L - mu|)
+// holds no entry that could enter a row's top-k, so the scan keeps the shortest
+// prefix of the order holding every tile that might.  One warp per voxel tile.
+__global__ void vt_steps_kernel(const float2* row_out, const float* vkey, const int32_t* vperm, int64_t n_vox,
+                                int64_t n_vtiles, const float* tlo, const float* thi, const uint16_t* order,
+                                int n_tiles, const float* lmax, uint16_t* steps) {
+    const int64_t vt = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (vt >= n_vtiles) return;
+    const float kmed = vkey[vperm[min(vt * TILE_M + TILE_M / 2, n_vox - 1)]];
+    float W = 0.f, B = 0.f;
+    for (int r = lane; r < TILE_M; r += 32) {
+        const int64_t pos = vt * TILE_M + r;
+        if (pos >= n_vox) break;
+        W = fmaxf(W, fabsf(vkey[vperm[pos]] - kmed));
+        const float b = row_out[pos].y;
+        B = fmaxf(B, b < 3.0e38f ? b : 3.0e38f);     // NaN (no probe result) -> no bound
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        W = fmaxf(W, __shfl_xor_sync(0xffffffffu, W, o));
+        B = fmaxf(B, __shfl_xor_sync(0xffffffffu, B, o));
+    }
+    B += U_BF16 * lmax[0];
+    const float slack = 1e-4f * (1.f + fabsf(kmed) + W);      // fp32 keys and |pc| = 1 to ~1e-6
+    int need = 0;                                   // scan positions [0, need) may hold a candidate
+    for (int base = 0; base < n_tiles; base += 32) {
+        const int i = base + lane;
+        bool keep = false;
+        if (i < n_tiles) {
+            const int o = order[vt * n_tiles + i];
+            const float d = fmaxf(0.f, fmaxf(tlo[o] - kmed, kmed - thi[o]));
+            keep = !((d - W) * (1.f - 1e-5f) - slack > B);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (m) need = base + 32 - __clz(m);
+    }
+    if (lane == 0) {
+        const int full = (n_tiles + PAIR - 1) / PAIR;
+        steps[vt] = (uint16_t)max(1, min(full, (need + PAIR - 1) / PAIR));
+    }
+}
+
 // Scan order of the library tiles for each voxel tile: the tile holding the
 // voxel tile's median key first, then outward by key distance.
 __global__ void order_kernel(const float* vkey, const int32_t* vperm, int64_t n_vox, int64_t n_vtiles,
-                             const float* tlo, const float* thi, int n_tiles, int sorted, uint16_t* order) {
+                             const float* tlo, const float* thi, int n_tiles, uint16_t* order) {
     const int64_t vt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (vt >= n_vtiles) return;
     uint16_t* o = order + vt * n_tiles;
-    if (!sorted) {
-        for (int s = 0; s < n_tiles; ++s) o[s] = (uint16_t)s;
-        return;
-    }
     const float key = vkey[vperm[min(vt * TILE_M + TILE_M / 2, n_vox - 1)]];
     int t0 = 0;
     while (t0 < n_tiles - 1 && thi[t0] < key) ++t0;
@@ -550,9 +587,11 @@ MADI_DEV void bitonic_clean(float (&a)[K], int (&ai)[K]) {
 // MB at a time; every lane of the warp takes part.  Buffer entry e of the
 // thread lives at buf[e * EPI_THREADS].  With the batch b sorted ascending and
 // padded with +inf to length K, min(ks[i], b[K-1-i]) holds the K smallest of
-// both lists as a bitonic sequence; only i >= K - MB can change.
+// both lists as a bitonic sequence; only i >= K - MB can change.  The new
+// threshold is the K-th best so far, or thr0 (a bound on the row's final K-th
+// best) when that is tighter.
 template <int K, int MB>
-MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, const float2* buf) {
+MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, const float2* buf, float thr0) {
     const int cmax = __reduce_max_sync(0xffffffffu, cnt);
 #pragma unroll 1
     for (int base = 0; base < cmax; base += MB) {
@@ -574,7 +613,7 @@ MADI_DEV void merge_buffer(float (&ks)[K], int (&kj)[K], float& thr, int& cnt, c
         bitonic_clean<K>(ks, kj);
     }
     cnt = 0;
-    thr = ks[K - 1];
+    thr = fminf(ks[K - 1], thr0);
 }
 
 // One append pass: up to four marked entries from each of two masks (column
@@ -613,8 +652,12 @@ MADI_DEV void append_pass(uint32_t& ma, int oa, uint32_t& mb, int ob, float2*& w
 //   accf[a]             : accumulator a holds tile scores (and, in the aux and
 //                         free modes, the tile's aux row has landed)
 //   acce[a]             : the eight epilogue warps are done with accumulator a
-//   afull               : the voxel tile (A operand) is written (warpgroup 0)
-//   lfull               : warpgroup 1's rescored best per row is written
+//   afull               : a voxel tile (A operand, two buffers) is written
+//                         (warpgroup 0, during the previous voxel tile's first step)
+//   lfull, lempty       : probe launch, end of a voxel tile: warpgroup 1's
+//                         top-k is in its buffer slots / warpgroup 0 has read
+//                         it (warpgroup 1 waits for that before going on, so
+//                         lfull never completes two phases ahead of its waiter)
 // Tile sequence g runs over (voxel tile of this CTA, library tile); stage
 // g % STAGES, accumulator g % ACCS.  The k-th completion of a barrier is
 // waited with parity k & 1.
@@ -630,7 +673,13 @@ struct Plan {
     const int32_t* vperm;               // voxel tile rows -> caller's voxel rows
     const int32_t* lperm;               // library scan position -> caller's library rows
     const float* lrows;                 // fp32 library rows in scan order, KPAD floats each
-    const uint16_t* order;              // [voxel tile][step] -> library tile
+    const uint16_t* order;              // [voxel tile][scan position] -> library tile
+    const uint16_t* vt_steps;           // steps of each voxel tile (a prefix of its scan); null = all
+    const float2* row_thr;              // per scan row: (k-th best score bound, -) from the probe; or null
+    float2* row_out;                    // probe: per scan row (k-th best score bound, residual bound)
+    const float* lmax;                  // max over the library of |L - mu| (fixed S0), device scalar
+    int probe;                          // 1: first step of every voxel tile only, write row_out, no candidates
+    int32_t* cand;                      // [scan row][half][k] candidate scan positions, -1 terminated
     int32_t* best_idx;
     float* best_resid;
     float* best_s0;
@@ -639,12 +688,11 @@ struct Plan {
 };
 
 struct Smem {
-    unsigned char a[A_BYTES];
+    unsigned char a[2][A_BYTES];                 // voxel tiles (A operand) of consecutive voxel tiles
     unsigned char b[STAGES][PAIR * B_BYTES];     // a step's two tiles back to back = one 256-row operand
     float aux[ACCS][PAIR][TILE_N];
     float4 stage[WG_COLS / 4][EPI_THREADS];   // the 64 keys of the current tile, 4 per slot
     float2 buf[CAP][EPI_THREADS];       // candidate buffers (score, index)
-    float4 res1[2][TILE_M];             // warpgroup 1 -> 0: (resid, index, s0, -) per row
     uint2 thr_pub[EPI_WG][TILE_M];      // (voxel tile, k-th best score) of each row and half
     uint64_t full[STAGES];
     uint64_t accf[ACCS];
@@ -652,6 +700,7 @@ struct Smem {
     int lt_stage[STAGES][PAIR];         // library tiles held by each stage (producer only)
     uint64_t afull;
     uint64_t lfull;
+    uint64_t lempty;
     uint64_t drain;
     uint64_t never;                     // no thread ever arrives (the test-only stalled wait)
     int64_t n_loaded, n_issued;         // producer: steps whose copies / MMAs were issued
@@ -661,10 +710,23 @@ struct Smem {
 
 MADI_DEV int err_flag_read(const Smem& S) { return *reinterpret_cast<const volatile int*>(&S.err); }
 
+// |m~|^2 of the BF16 row the MMA sees (m~ = bf16(m - mu), as write_voxel_tile
+// rounds it) and |m - mu|^2 in fp32, for the fixed-S0 bounds.
+MADI_DEV void row_norms(const Plan& P, int64_t row, float& mh2, float& mn2) {
+    mh2 = 0.f;
+    mn2 = 0.f;
+    for (int k = 0; k < P.F; ++k) {
+        const float x = P.meas[row * P.F + k] - __ldg(P.mu + k);
+        const float xb = __bfloat162float(__float2bfloat16_rn(x));
+        mh2 = fmaf(xb, xb, mh2);
+        mn2 = fmaf(x, x, mn2);
+    }
+}
+
 // Voxel tile -> BF16 canonical A rows (warpgroup 0, each thread its own row),
 // then hand the tile to the async proxy and signal the producer.
 template <int MODE>
-MADI_DEV void write_voxel_tile(Smem& S, const Plan& P, int64_t vt, int r, int lane) {
+MADI_DEV void write_voxel_tile(Smem& S, const Plan& P, int64_t vt, int buf, int r, int lane) {
     const int64_t pos = vt * TILE_M + r;
     const bool live = pos < P.n_vox;
     const int64_t row = live ? P.vperm[pos] : 0;
@@ -678,40 +740,33 @@ MADI_DEV void write_voxel_tile(Smem& S, const Plan& P, int64_t vt, int r, int la
             if (MODE == MODE_FOLD && k >= P.F && k < P.F + BIAS_COLS) x = 1.f;
             v8[i] = __float2bfloat16_rn(x);
         }
-        *reinterpret_cast<uint4*>(S.a + canon_off(r, kc * 8)) = *reinterpret_cast<const uint4*>(v8);
+        *reinterpret_cast<uint4*>(S.a[buf] + canon_off(r, kc * 8)) = *reinterpret_cast<const uint4*>(v8);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic -> async proxy
     __syncwarp();
     if (lane == 0) mbar_arrive(&S.afull);
 }
 
-// The producer is a whole warp so that the scan order can be read 32 tiles at
-// a time (one coalesced load per lane, double-buffered, picked by shuffle);
-// lane 0 alone waits on barriers and issues the copies and MMAs.  Step g
-// covers tiles 2g and 2g + 1 of the padded per-voxel-tile sequence (an odd
-// tile count is padded with the all-padding tile n_tiles).
+// Steps (library tile pairs, a prefix of the scan order) of voxel tile vt.
+MADI_DEV int vtile_steps(const Plan& P, int64_t vt) {
+    const int full = (P.n_tiles + PAIR - 1) / PAIR;
+    if (P.probe) return 1;
+    return P.vt_steps ? (int)P.vt_steps[vt] : full;
+}
+
+// Library tile at scan position i of voxel tile vt (the all-padding tile past the end).
+MADI_DEV int scan_tile(const Plan& P, int64_t vt, int i) {
+    return i < P.n_tiles ? (int)P.order[vt * P.n_tiles + i] : P.n_tiles;
+}
+
+// Lane 0 of the producer warp waits on barriers and issues the copies and
+// MMAs.  The step sequence runs over this CTA's voxel tiles, each for its
+// vtile_steps; step g covers scan positions 2s and 2s + 1 of its voxel tile
+// (an odd tile count is padded with the all-padding tile n_tiles).  The scan
+// order entries of a load are read one load ahead.
 template <int MODE>
-MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int lane) {
-    const int n_tiles = P.n_tiles, n_pad = PAIR * ((n_tiles + PAIR - 1) / PAIR);
-    const int64_t n_q = total * PAIR;
-    auto order_at = [&](int64_t q) -> int {    // library tile of padded position q, 0 past the end
-        if (q >= n_q) return 0;
-        const int64_t vt = blockIdx.x + (q / n_pad) * (int64_t)gridDim.x;
-        const int i = (int)(q % n_pad);
-        return i < n_tiles ? (int)P.order[vt * n_tiles + i] : n_tiles;
-    };
-    int64_t obase = 0;                           // positions [obase, obase + 32) are in ocur
-    int ocur = order_at(lane), onext = order_at(32 + lane);
-    auto lib_tile = [&](int64_t q) -> int {      // warp-uniform, q never decreases
-        while (q >= obase + 32) {
-            ocur = onext;
-            obase += 32;
-            onext = order_at(obase + 32 + lane);
-        }
-        return __shfl_sync(0xffffffffu, ocur, (int)(q - obase));
-    };
+MADI_DEV void producer(Smem& S, const Plan& P, int64_t my_vt, uint32_t tmem, int lane) {
     const uint32_t idesc = make_idesc();
-    const uint32_t a_base = smem_u32(S.a);
     int64_t gl = 0;                                  // steps loaded
     bool ok = true;
     // The stage refilled with step g + LOAD_AHEAD last held step
@@ -719,27 +774,46 @@ MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int
     // refill certifies the epilogue of step g - ACCS, hence that MMA's (and all
     // earlier MMAs') completion, so the stage is free without a barrier of its own.
     static_assert(STAGES - LOAD_AHEAD >= ACCS, "a refilled stage must be certified free by the acce wait");
-    auto load = [&](int64_t g) {
-        const int st = (int)(g % STAGES);
-        const int lt0 = lib_tile(PAIR * g), lt1 = lib_tile(PAIR * g + 1);
-        if (lane == 0) {
+    if (lane == 0) {
+        int64_t total = 0;
+        for (int64_t lv = 0; lv < my_vt; ++lv) total += vtile_steps(P, blockIdx.x + lv * (int64_t)gridDim.x);
+        // load cursor (voxel tile slot, step, steps of that tile) and the next load's tiles
+        int64_t l_lv = 0;
+        int l_s = 0, l_n = my_vt > 0 ? vtile_steps(P, blockIdx.x) : 0;
+        int nt0 = 0, nt1 = 0;
+        auto fetch = [&]() {
+            if (l_lv < my_vt) {
+                const int64_t vt = blockIdx.x + l_lv * (int64_t)gridDim.x;
+                nt0 = scan_tile(P, vt, PAIR * l_s);
+                nt1 = scan_tile(P, vt, PAIR * l_s + 1);
+            }
+        };
+        fetch();
+        auto load = [&](int64_t g) {
+            const int st = (int)(g % STAGES);
+            const int lt0 = nt0, lt1 = nt1;
+            if (++l_s == l_n) {
+                l_s = 0;
+                ++l_lv;
+                l_n = l_lv < my_vt ? vtile_steps(P, blockIdx.x + l_lv * (int64_t)gridDim.x) : 0;
+            }
+            fetch();                                 // the next load's tiles, a whole step ahead
             S.lt_stage[st][0] = lt0;
             S.lt_stage[st][1] = lt1;
             mbar_expect_tx(&S.full[st], PAIR * B_BYTES);
             bulk_g2s(S.b[st], P.tiles + (size_t)lt0 * B_BYTES, B_BYTES, &S.full[st]);
             bulk_g2s(S.b[st] + B_BYTES, P.tiles + (size_t)lt1 * B_BYTES, B_BYTES, &S.full[st]);
-        }
-    };
-    const int64_t n_steps = n_pad / PAIR;
-    for (; gl < total && gl < LOAD_AHEAD; ++gl) load(gl);
-    int64_t g = 0;                                   // steps whose MMAs were issued
-    for (; g < total && ok; ++g) {
-        const int st = (int)(g % STAGES), acc = (int)(g % ACCS);
-        if (g >= ACCS && !mbar_wait_warp(&S.acce[acc], (uint32_t)((g / ACCS - 1) & 1), lane)) { ok = false; break; }
-        if (gl < total && gl <= g + LOAD_AHEAD) load(gl++);
-        if (g % n_steps == 0 && !mbar_wait_warp(&S.afull, (uint32_t)((g / n_steps) & 1), lane)) { ok = false; break; }
-        if (!mbar_wait_warp(&S.full[st], (uint32_t)((g / STAGES) & 1), lane)) { ok = false; break; }
-        if (lane == 0) {
+        };
+        for (; gl < total && gl < LOAD_AHEAD; ++gl) load(gl);
+        int64_t g = 0;                               // steps whose MMAs were issued
+        int64_t m_lv = 0;                            // MMA cursor
+        int m_s = 0, m_n = my_vt > 0 ? vtile_steps(P, blockIdx.x) : 0;
+        for (; g < total && ok; ++g) {
+            const int st = (int)(g % STAGES), acc = (int)(g % ACCS);
+            if (g >= ACCS && !mbar_wait(&S.acce[acc], (uint32_t)((g / ACCS - 1) & 1), SPIN_LIMIT)) { ok = false; break; }
+            if (gl < total && gl <= g + LOAD_AHEAD) load(gl++);
+            if (m_s == 0 && !mbar_wait(&S.afull, (uint32_t)(m_lv & 1), SPIN_LIMIT)) { ok = false; break; }
+            if (!mbar_wait(&S.full[st], (uint32_t)((g / STAGES) & 1), SPIN_LIMIT)) { ok = false; break; }
             fence_after();
             if (MODE != MODE_FOLD) {
                 // the step's aux rows ride on accf[acc] (arrive + tx); the MMA commit is its second arrival
@@ -747,19 +821,23 @@ MADI_DEV void producer(Smem& S, const Plan& P, int64_t total, uint32_t tmem, int
                 bulk_g2s(S.aux[acc][0], P.aux + (size_t)S.lt_stage[st][0] * TILE_N, AUX_BYTES, &S.accf[acc]);
                 bulk_g2s(S.aux[acc][1], P.aux + (size_t)S.lt_stage[st][1] * TILE_N, AUX_BYTES, &S.accf[acc]);
             }
+            const uint32_t a_base = smem_u32(S.a[m_lv & 1]);
             const uint32_t b_base = smem_u32(S.b[st]);
             const uint32_t d = tmem + (uint32_t)(acc * MMA_N);
             mma_bf16(d, make_sdesc(a_base), make_sdesc(b_base), idesc, 0u);
             mma_bf16(d, make_sdesc(a_base + 2 * LBO), make_sdesc(b_base + 2 * LBO), idesc, 1u);
             mma_commit(&S.accf[acc]);
+            if (++m_s == m_n) {
+                m_s = 0;
+                ++m_lv;
+                m_n = m_lv < my_vt ? vtile_steps(P, blockIdx.x + m_lv * (int64_t)gridDim.x) : 0;
+            }
         }
-        __syncwarp();
-    }
-    if (lane == 0) {
         S.n_loaded = gl;
         S.n_issued = g;
         if (!ok) S.err = ERR_TIMEOUT;
     }
+    __syncwarp();
 }
 
 // After an error (the epilogue may have left before consuming every step):
@@ -785,63 +863,70 @@ MADI_DEV bool drain_issued(Smem& S) {
     return mbar_wait(&S.drain, 0, DRAIN_LIMIT) && ok;
 }
 
-// fp32 rescore of this thread's k candidates (staged in its buffer, as scan
-// positions) against the fp32 data; lowest caller index on ties.  Rows come
-// from the padded scan-order copy (RQ aligned 16-byte loads each, RQ >= F/4),
-// NC candidates per step with all their loads in flight.
-template <int K, bool FREE, int RQ, int NC>
-MADI_DEV void rescore_rows(const Plan& P, int64_t row, const float2* mybuf, int nv, float& best, int& bj,
-                           float& bs0) {
+// fp32 rescore of the candidates of one voxel against the fp32 data; lowest
+// caller index on ties.  Two adjacent threads take the voxel, one per half's
+// list (scan positions, a prefix of its K slots with -1 after it), and combine
+// their bests by shuffle.  Library rows come from the padded scan-order copy
+// (RQ aligned 16-byte loads each, RQ >= F/4), two candidates per round with
+// all their loads in flight; many warps per SM cover the latency.
+template <int K, bool FREE, int RQ>
+__global__ void __launch_bounds__(256, 2) rescore_kernel(const Plan P) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t pos = t >> 1;
+    const int h = (int)(t & 1);
+    const bool live = pos < P.n_vox;
+    const int64_t row = live ? P.vperm[pos] : 0;
     const int F = P.F, nq = (F + 3) / 4;
     float m[4 * RQ];
 #pragma unroll
-    for (int k = 0; k < 4 * RQ; ++k) m[k] = k < F ? P.meas[row * F + k] : 0.f;
+    for (int k = 0; k < 4 * RQ; ++k) m[k] = live && k < F ? P.meas[row * F + k] : 0.f;
+    float best = 3.0e38f, bs0 = 0.f;
+    int bj = 0x7FFFFFFF;
+    const int4* cand = reinterpret_cast<const int4*>(P.cand + (live ? pos : 0) * (EPI_WG * K) + h * K);
 #pragma unroll 1
-    for (int i = 0; i < nv; i += NC) {
-        int e[NC], j[NC];
-        float4 lv[NC][RQ];
+    for (int q4 = 0; live && q4 < K / 4; ++q4) {
+        const int4 c4 = cand[q4];
+        const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-        for (int u = 0; u < NC; ++u) {
-            const float2 c = (i + u < nv) ? mybuf[(i + u) * EPI_THREADS] : make_float2(__int_as_float(-1), 0.f);
-            e[u] = __float_as_int(c.x);
-            j[u] = __float_as_int(c.y);
-            const float4* L = reinterpret_cast<const float4*>(P.lrows + (size_t)(e[u] < 0 ? 0 : e[u]) * KPAD);
+        for (int p2 = 0; p2 < 4; p2 += 2) {
+            int e[2], j[2];
+            float4 lv[2][RQ];
 #pragma unroll
-            for (int q = 0; q < RQ; ++q)
-                lv[u][q] = (e[u] >= 0 && q < nq) ? __ldg(L + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int u = 0; u < 2; ++u) {
+                const int c = cc[p2 + u];
+                e[u] = c >= 0 && c < P.n_lib ? c : -1;
+                j[u] = e[u] >= 0 ? __ldg(P.lperm + e[u]) : -1;
+                const float4* L = reinterpret_cast<const float4*>(P.lrows + (size_t)(e[u] < 0 ? 0 : e[u]) * KPAD);
+#pragma unroll
+                for (int q = 0; q < RQ; ++q)
+                    lv[u][q] = (e[u] >= 0 && q < nq) ? __ldg(L + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (e[u] < 0) continue;
+                const float* lf = reinterpret_cast<const float*>(lv[u]);
+                float dot = 0.f, rr = 0.f;
+#pragma unroll
+                for (int k = 0; k < 4 * RQ; ++k) { dot = fmaf(m[k], lf[k], dot); rr = fmaf(lf[k], lf[k], rr); }
+                const float s0 = FREE ? dot / fmaxf(rr, 1e-30f) : 1.f;
+                float res = 0.f;
+#pragma unroll
+                for (int k = 0; k < 4 * RQ; ++k) { const float r = m[k] - s0 * lf[k]; res = fmaf(r, r, res); }
+                if (FREE && !(dot > 0.f)) res = 3.0e38f;
+                if (res < best || (res == best && j[u] < bj)) { best = res; bj = j[u]; bs0 = s0; }
+            }
         }
-#pragma unroll
-        for (int u = 0; u < NC; ++u) {
-            if (e[u] < 0) continue;
-            const float* lf = reinterpret_cast<const float*>(lv[u]);
-            float dot = 0.f, rr = 0.f;
-#pragma unroll
-            for (int k = 0; k < 4 * RQ; ++k) { dot = fmaf(m[k], lf[k], dot); rr = fmaf(lf[k], lf[k], rr); }
-            const float s0 = FREE ? dot / fmaxf(rr, 1e-30f) : 1.f;
-            float res = 0.f;
-#pragma unroll
-            for (int k = 0; k < 4 * RQ; ++k) { const float r = m[k] - s0 * lf[k]; res = fmaf(r, r, res); }
-            if (FREE && !(dot > 0.f)) res = 3.0e38f;
-            if (res < best || (res == best && j[u] < bj)) { best = res; bj = j[u]; bs0 = s0; }
-        }
+        if (c4.w < 0) break;
     }
-}
-
-template <int K, bool FREE>
-MADI_DEV void rescore(const Plan& P, int64_t row, const float2* mybuf, int nv, float& best, int& bj, float& bs0) {
-    // all K permutation lookups in flight at once; (scan position, caller index)
-    // go back into the thread's buffer slots
-    float2* wbuf = const_cast<float2*>(mybuf);
-#pragma unroll
-    for (int i = 0; i < K; ++i) {
-        const float2 cand = mybuf[i * EPI_THREADS];
-        const int e = __float_as_int(cand.y);
-        const bool valid = i < nv && cand.x < 3.0e38f && e >= 0 && e < P.n_lib;
-        const int j = valid ? __ldg(P.lperm + e) : -1;
-        wbuf[i * EPI_THREADS] = make_float2(__int_as_float(valid ? e : -1), __int_as_float(j));
-    }
-    if (P.F <= 24) rescore_rows<K, FREE, 6, 4>(P, row, mybuf, nv, best, bj, bs0);
-    else rescore_rows<K, FREE, KPAD / 4, 2>(P, row, mybuf, nv, best, bj, bs0);
+    // combine the two halves (lanes 2i, 2i + 1)
+    const float ob = __shfl_xor_sync(0xffffffffu, best, 1);
+    const int oj = __shfl_xor_sync(0xffffffffu, bj, 1);
+    const float os0 = __shfl_xor_sync(0xffffffffu, bs0, 1);
+    if (ob < best || (ob == best && oj < bj)) { best = ob; bj = oj; bs0 = os0; }
+    if (!live || h != 0 || bj == 0x7FFFFFFF) return;   // no candidates: the voxel's CTA gave up
+    P.best_idx[row] = bj;
+    P.best_resid[row] = best;
+    if (FREE && P.best_s0) P.best_s0[row] = bs0;
 }
 
 template <int K, int MODE>
@@ -860,13 +945,16 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
         }
         mbar_init(&S.afull, 4);
         mbar_init(&S.lfull, 4);
+        mbar_init(&S.lempty, 4);
         mbar_init(&S.drain, 1);
         mbar_init(&S.never, 1);
         S.n_loaded = 0;
         S.n_issued = 0;
         S.err = 0;
     }
-    if (tid < EPI_THREADS) S.thr_pub[tid / TILE_M][tid % TILE_M] = make_uint2(0xFFFFFFFFu, 0u);
+    if (tid < EPI_THREADS) {
+        S.thr_pub[tid / TILE_M][tid % TILE_M] = make_uint2(0xFFFFFFFFu, 0u);
+    }
     if (tid == 0) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -881,11 +969,10 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
     const uint32_t tmem = S.tmem_base;
     const int64_t n_vtiles = (P.n_vox + TILE_M - 1) / TILE_M;
     const int n_tiles = P.n_tiles;
-    const int n_steps = (n_tiles + PAIR - 1) / PAIR;
     const int64_t my_vt = (int64_t)blockIdx.x < n_vtiles ? (n_vtiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
     if (warp == EPI_WARPS) {
-        producer<MODE>(S, P, my_vt * n_steps, tmem, lane);
+        producer<MODE>(S, P, my_vt, tmem, lane);
     } else {
         const int wg = warp >> 2;                    // column half
         const int r = tid & (TILE_M - 1);            // voxel row = TMEM lane
@@ -895,19 +982,27 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
         const float* mystage_f = reinterpret_cast<const float*>(mystage);
         int64_t g = 0;
         bool ok = true;
-        if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, P, blockIdx.x, r, lane);
+        if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, P, blockIdx.x, 0, r, lane);
         if (P.test_stall && my_vt > 0 && !mbar_wait_warp(&S.never, 0, lane, STALL_POLLS)) {
             S.err = ERR_TIMEOUT;    // tests only: the wait runs out like any other would
             ok = false;
         }
         for (int64_t lv = 0; lv < my_vt && ok; ++lv) {
             const int64_t vt = blockIdx.x + lv * gridDim.x;
+            const int n_steps = vtile_steps(P, vt);
+            const int64_t pos = vt * TILE_M + r;
             float ks[K];
             int kj[K];
 #pragma unroll
             for (int i = 0; i < K; ++i) { ks[i] = 3.0e38f; kj[i] = 0; }
-            float thr = 3.0e38f;
-            float tthr = -1.5e38f;                   // fold mode: key t hits when t > -thr / 2
+            // the probe's bound on this row's final k-th best score (no effect when absent)
+            float thr0 = 3.0e38f;
+            if (P.row_thr && pos < P.n_vox) {
+                const float b = P.row_thr[pos].x;
+                thr0 = b < 3.0e38f ? b : 3.0e38f;            // NaN (no probe result) -> no bound
+            }
+            float thr = thr0;
+            float tthr = -0.5f * thr;                // fold mode: key t hits when t > -thr / 2
             int cnt = 0;
             // library tile of this warpgroup at step t (the padding tile past the end)
             auto my_tile = [&](int t) -> int {
@@ -958,7 +1053,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                     bitonic_sort<K>(sk, sj);
 #pragma unroll
                     for (int i = 0; i < K; ++i) { ks[i] = sk[i]; kj[i] = sj[i]; }
-                    thr = ks[K - 1];
+                    thr = fminf(ks[K - 1], thr0);
                     tthr = -0.5f * thr;
                     S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
                     seeded = K >= 32 ? 0xFFFFFFFFu : ((1u << K) - 1u);
@@ -1008,7 +1103,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                         // fold before each half as needed, then append it
                         uint32_t none = 0u;
                         if (__any_sync(0xffffffffu, cnt + nh0 > CAP)) {
-                            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
+                            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
                             tthr = -0.5f * thr;
                             S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
                             wp = mybuf_w;
@@ -1016,7 +1111,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                         while (__any_sync(0xffffffffu, m0 != 0u)) append_pass<MODE>(m0, 0, none, 0, wp, mystage_f, jb);
                         cnt += nh0;
                         if (__any_sync(0xffffffffu, cnt + nh1 > CAP)) {
-                            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
+                            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
                             tthr = -0.5f * thr;
                             S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
                             wp = mybuf_w;
@@ -1025,15 +1120,57 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                         cnt += nh1;
                     }
                 }
+                // After the first step, the next voxel tile's A goes into the other
+                // buffer: its last reader, the previous voxel tile's MMAs, completed
+                // before this tile's first step did, and the producer has already
+                // waited on this tile's afull phase, so afull never runs two phases
+                // ahead of its waiter.
+                if (t == 0 && wg == 0 && lv + 1 < my_vt)
+                    write_voxel_tile<MODE>(S, P, vt + gridDim.x, (int)((lv + 1) & 1), r, lane);
                 fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.acce[acc]);
             }
             if (!ok) break;
-            // every MMA of this voxel tile is complete: the next tile's A may go in now
-            if (wg == 0 && lv + 1 < my_vt) write_voxel_tile<MODE>(S, P, vt + gridDim.x, r, lane);
-            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf);
+            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
             S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+            const int64_t row = pos < P.n_vox ? P.vperm[pos] : -1;
+            if (P.probe) {
+                // The row's k-th best over the step's two tiles bounds its final
+                // k-th best: (score bound, residual bound) for the step counts.
+                // Warpgroup 1 hands its ascending top-k over in its own buffer
+                // slots and waits until warpgroup 0 has read them.
+                if (wg == 1) {
+#pragma unroll
+                    for (int i = 0; i < K; ++i) mybuf_w[i * EPI_THREADS] = make_float2(ks[i], 0.f);
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.lfull);
+                    if (!mbar_wait_warp(&S.lempty, (uint32_t)(lv & 1), lane)) { S.err = ERR_TIMEOUT; ok = false; break; }
+                } else {
+                    if (!mbar_wait_warp(&S.lfull, (uint32_t)(lv & 1), lane)) { S.err = ERR_TIMEOUT; ok = false; break; }
+                    // k-th smallest of the union of the two ascending lists:
+                    // min over i of max(ks[i - 1], other[k - 1 - i])
+                    const float2* other = &S.buf[0][TILE_M + r];
+                    float t = 3.0e38f;
+#pragma unroll
+                    for (int i = 0; i <= K; ++i) {
+                        const float a = i > 0 ? ks[i - 1] : -3.0e38f;
+                        const float b = i < K ? other[(K - 1 - i) * EPI_THREADS].x : -3.0e38f;
+                        t = fminf(t, fmaxf(a, b));
+                    }
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.lempty);
+                    if (row >= 0) {
+                        float mh2, mn2;
+                        row_norms(P, row, mh2, mn2);
+                        const float lm = __ldg(P.lmax);
+                        const float r2 = t + mh2 + 1e-5f * (1.f + mh2 + lm * lm);
+                        const float rb = sqrtf(fmaxf(r2, 0.f)) * (1.f + 1e-5f) + U_BF16 * sqrtf(mn2);
+                        P.row_out[pos] = make_float2(t + fmaxf(fabsf(t) * 1e-6f, 1e-12f), rb);
+                    }
+                }
+                continue;
+            }
             // Candidates above the other half's k-th best cannot be in the row's
             // overall top-k; ks is ascending, so the rest is a prefix of length nv
             // (a stale partner value only keeps more).
@@ -1042,29 +1179,13 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
             int nv = 0;
 #pragma unroll
             for (int i = 0; i < K; ++i) nv += (ks[i] < 3.0e38f && ks[i] <= cut) ? 1 : 0;
-            // the (now empty) buffer carries the candidates to the rescore loop, so
-            // ks/kj are only ever indexed by constants and stay in registers
+            // candidates (scan positions, ascending BF16 score) for the rescore kernel
+            if (row >= 0) {
+                int4* c = reinterpret_cast<int4*>(P.cand + (pos * EPI_WG + wg) * K);
 #pragma unroll
-            for (int i = 0; i < K; ++i) mybuf_w[i * EPI_THREADS] = make_float2(ks[i], __int_as_float(kj[i]));
-            const int64_t pos = vt * TILE_M + r;
-            const int64_t row = pos < P.n_vox ? P.vperm[pos] : -1;
-            float best = 3.0e38f, bs0 = 0.f;
-            int bj = 0x7FFFFFFF;
-            if (row >= 0) rescore<K, FREE>(P, row, mybuf, nv, best, bj, bs0);
-            if (wg == 1) {
-                S.res1[lv & 1][r] = make_float4(best, __int_as_float(bj), bs0, 0.f);
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&S.lfull);
-            } else {
-                if (!mbar_wait_warp(&S.lfull, (uint32_t)(lv & 1), lane)) { S.err = ERR_TIMEOUT; ok = false; break; }
-                const float4 o = S.res1[lv & 1][r];
-                const int j1 = __float_as_int(o.y);
-                if (o.x < best || (o.x == best && j1 < bj)) { best = o.x; bj = j1; bs0 = o.z; }
-                if (row >= 0) {
-                    P.best_idx[row] = bj == 0x7FFFFFFF ? 0 : bj;
-                    P.best_resid[row] = best;
-                    if (FREE && P.best_s0) P.best_s0[row] = bs0;
-                }
+                for (int i = 0; i < K; i += 4)
+                    c[i / 4] = make_int4(i < nv ? kj[i] : -1, i + 1 < nv ? kj[i + 1] : -1, i + 2 < nv ? kj[i + 2] : -1,
+                                         i + 3 < nv ? kj[i + 3] : -1);
             }
         }
     }
@@ -1096,10 +1217,11 @@ namespace {
 // Scratch layout of the BF16 path (every part 256-byte aligned).
 struct Layout {
     int64_t tiles, aux, mu, err, kmu, pc, cov, lkey, lperm, krange, tlo, thi;
-    int64_t lrows, vkey, vb, vrank, cnt, offs, vtot, vperm, order, total;
+    int64_t lrows, vkey, vb, vrank, cnt, offs, vtot, vperm, order, rowout, vsteps, lmax, cand;
+    int64_t lvb, lvrank, lcnt, loffs, ltot, total;
 };
 
-Layout layout(int64_t n_vox, int64_t n_lib) {
+Layout layout(int64_t n_vox, int64_t n_lib, int topk) {
     const int64_t n_tiles = (n_lib + TILE_N - 1) / TILE_N;
     const int64_t n_pad = PAIR * ((n_tiles + PAIR - 1) / PAIR);   // + the all-padding tile when odd
     const int64_t n_vtiles = (n_vox + TILE_M - 1) / TILE_M;
@@ -1128,6 +1250,16 @@ Layout layout(int64_t n_vox, int64_t n_lib) {
     L.vtot = take(NBUCKET * 4);
     L.vperm = take(n_vox * 4);
     L.order = take(n_vtiles * n_tiles * 2);
+    L.rowout = take(n_vtiles * TILE_M * 8);
+    L.vsteps = take(n_vtiles * 2);
+    L.lmax = take(4);
+    L.cand = take(n_vox * EPI_WG * topk * 4);
+    const int64_t lnblk = (n_lib + VBLK - 1) / VBLK;
+    L.lvb = take(n_lib);
+    L.lvrank = take(n_lib * 2);
+    L.lcnt = take(lnblk * NBUCKET * 4);
+    L.loffs = take(lnblk * NBUCKET * 4);
+    L.ltot = take(NBUCKET * 4);
     L.total = off;
     return L;
 }
@@ -1136,13 +1268,14 @@ unsigned blocks_for(int64_t n, int per) { return (unsigned)((n + per - 1) / per)
 }  // namespace
 
 int64_t madi_match_bf16_scratch(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t topk) {
-    (void)n_feat; (void)topk;
-    return layout(n_vox, n_lib).total;
+    (void)n_feat;
+    return layout(n_vox, n_lib, topk).total;
 }
 
 // Device address of the status word madi_match_bf16 left in the scratch.
 const int* madi_match_bf16_status_word(const madi_match_desc* d) {
-    return reinterpret_cast<const int*>(static_cast<const unsigned char*>(d->scratch) + layout(d->n_vox, d->n_lib).err);
+    return reinterpret_cast<const int*>(static_cast<const unsigned char*>(d->scratch) +
+                                        layout(d->n_vox, d->n_lib, d->topk).err);
 }
 
 // Library column means (fp64 sums), shared with the fp32 fixed-S0 scan.
@@ -1156,7 +1289,7 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     const int64_t n_tiles64 = ((int64_t)d->n_lib + TILE_N - 1) / TILE_N;
     if (d->n_vox >= (int64_t(1) << 31) || n_tiles64 > 65535)
         return host::fail(MADI_ERR_UNSUPPORTED, "match bf16: at most 2^31-1 voxels and 65535 library tiles");
-    const Layout Ly = layout(d->n_vox, d->n_lib);
+    const Layout Ly = layout(d->n_vox, d->n_lib, d->topk);
     if (!d->scratch || d->scratch_bytes < Ly.total)
         return host::fail(MADI_ERR_CAPACITY, "match bf16: scratch %lld < %lld bytes", (long long)d->scratch_bytes,
                           (long long)Ly.total);
@@ -1188,38 +1321,46 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     uint16_t* order = reinterpret_cast<uint16_t*>(at(Ly.order));
     int* err = reinterpret_cast<int*>(at(Ly.err));
 
+    float* lmax = reinterpret_cast<float*>(at(Ly.lmax));
+    float2* rowout = reinterpret_cast<float2*>(at(Ly.rowout));
+    uint16_t* vsteps = reinterpret_cast<uint16_t*>(at(Ly.vsteps));
     cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(lmax, 0, sizeof(float), s);
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");
     if (!free_s0) column_mean_kernel<<<F, 256, 0, s>>>(d->lib, n_lib, F, mu);
-    // ---- scan order: library sorted along its principal axis, voxels bucketed ----
-    const bool sorted = n_lib <= SORT_MAX;
-    if (sorted) {
-        key_mean_kernel<<<F, 256, 0, s>>>(d->lib, n_lib, F, unit, kmu);
-        key_cov_kernel<<<F * F, 256, 0, s>>>(d->lib, n_lib, F, unit, kmu, cov);
-        key_axis_kernel<<<1, 32, 0, s>>>(cov, F, pc);
-        key_kernel<<<blocks_for(n_lib, 256), 256, 0, s>>>(d->lib, n_lib, F, unit, kmu, pc, lkey);
-        int n2 = 1;
-        while (n2 < n_lib) n2 <<= 1;
-        e = cudaFuncSetAttribute(lib_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SORT_MAX * 4);
-        if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 sort attribute");
-        lib_sort_kernel<<<1, 1024, (size_t)n2 * 4, s>>>(lkey, n_lib, lperm, krange);
-        tile_bounds_kernel<<<blocks_for(n_tiles, 256), 256, 0, s>>>(lkey, lperm, n_lib, n_tiles, tlo, thi);
-        vox_bucket_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(d->measured, n_vox, F, unit, kmu, pc, krange, vkey, vb);
-        vox_rank_kernel<<<(unsigned)nblk, VBLK, 0, s>>>(vb, n_vox, vrank, cnt);
-        uint32_t* vtot = reinterpret_cast<uint32_t*>(at(Ly.vtot));
-        vox_scan_kernel<<<NBUCKET, 1024, 0, s>>>(cnt, (int)nblk, offs, vtot);
-        vox_base_kernel<<<1, 32, 0, s>>>(vtot);
-        vox_scatter_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(vb, vrank, offs, vtot, n_vox, (int)nblk, vperm);
-    } else {
-        iota_kernel<<<blocks_for(n_lib, 256), 256, 0, s>>>(lperm, n_lib);
-        iota_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(vperm, n_vox);
+    // ---- scan order: library and voxels bucketed along the library's principal axis ----
+    // (fixed S0 keys rows as they are, so their mean is the column mean)
+    const float* kmean = unit ? kmu : mu;
+    if (unit) key_mean_kernel<<<F, 256, 0, s>>>(d->lib, n_lib, F, unit, kmu);
+    key_cov_kernel<<<F * F, 256, 0, s>>>(d->lib, n_lib, F, unit, kmean, cov);
+    key_axis_kernel<<<1, 32, 0, s>>>(cov, F, pc);
+    key_kernel<<<blocks_for(n_lib, 256), 256, 0, s>>>(d->lib, n_lib, F, unit, kmean, pc, lkey);
+    key_range_kernel<<<1, 1024, 0, s>>>(lkey, n_lib, krange);
+    {
+        const int64_t lnblk = (n_lib + VBLK - 1) / VBLK;
+        uint8_t* lvb = reinterpret_cast<uint8_t*>(at(Ly.lvb));
+        uint16_t* lvrank = reinterpret_cast<uint16_t*>(at(Ly.lvrank));
+        uint32_t* lcnt = reinterpret_cast<uint32_t*>(at(Ly.lcnt));
+        uint32_t* loffs = reinterpret_cast<uint32_t*>(at(Ly.loffs));
+        uint32_t* ltot = reinterpret_cast<uint32_t*>(at(Ly.ltot));
+        key_bucket_kernel<<<blocks_for(n_lib, 256), 256, 0, s>>>(lkey, n_lib, krange, lvb);
+        vox_rank_kernel<<<(unsigned)lnblk, VBLK, 0, s>>>(lvb, n_lib, lvrank, lcnt);
+        vox_scan_kernel<<<NBUCKET, 1024, 0, s>>>(lcnt, (int)lnblk, loffs, ltot);
+        vox_base_kernel<<<1, 32, 0, s>>>(ltot);
+        vox_scatter_kernel<<<blocks_for(n_lib, 256), 256, 0, s>>>(lvb, lvrank, loffs, ltot, n_lib, (int)lnblk, lperm);
     }
-    order_kernel<<<blocks_for(n_vtiles, 128), 128, 0, s>>>(vkey, vperm, n_vox, n_vtiles, tlo, thi, n_tiles,
-                                                            sorted ? 1 : 0, order);
+    tile_bounds_kernel<<<blocks_for(n_tiles, 128), 128, 0, s>>>(lkey, lperm, n_lib, n_tiles, tlo, thi);
+    vox_bucket_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(d->measured, n_vox, F, unit, kmean, pc, krange, vkey, vb);
+    vox_rank_kernel<<<(unsigned)nblk, VBLK, 0, s>>>(vb, n_vox, vrank, cnt);
+    uint32_t* vtot = reinterpret_cast<uint32_t*>(at(Ly.vtot));
+    vox_scan_kernel<<<NBUCKET, 1024, 0, s>>>(cnt, (int)nblk, offs, vtot);
+    vox_base_kernel<<<1, 32, 0, s>>>(vtot);
+    vox_scatter_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(vb, vrank, offs, vtot, n_vox, (int)nblk, vperm);
+    order_kernel<<<blocks_for(n_vtiles, 128), 128, 0, s>>>(vkey, vperm, n_vox, n_vtiles, tlo, thi, n_tiles, order);
     const int n_pad = PAIR * ((n_tiles + PAIR - 1) / PAIR);
     pack_library_kernel<<<blocks_for((int64_t)n_pad * TILE_N, 256), 256, 0, s>>>(
         d->lib, n_lib, F, n_pad, mode, mu, lperm, reinterpret_cast<unsigned char*>(at(Ly.tiles)),
-        reinterpret_cast<float*>(at(Ly.aux)), reinterpret_cast<float*>(at(Ly.lrows)));
+        reinterpret_cast<float*>(at(Ly.aux)), reinterpret_cast<float*>(at(Ly.lrows)), lmax);
     e = cudaGetLastError();
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 preparation");
 
@@ -1237,6 +1378,8 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     P.lperm = lperm;
     P.lrows = reinterpret_cast<const float*>(at(Ly.lrows));
     P.order = order;
+    P.lmax = free_s0 ? nullptr : lmax;
+    P.cand = reinterpret_cast<int32_t*>(at(Ly.cand));
     P.best_idx = d->best_idx;
     P.best_resid = d->best_resid;
     P.best_s0 = d->best_s0;
@@ -1261,9 +1404,51 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
         else if (d->topk == 16) MADI_LAUNCH_BF16(16, MD);                                                 \
         else MADI_LAUNCH_BF16(32, MD);                                                                    \
     } while (0)
-    if (mode == MODE_FOLD) MADI_LAUNCH_BF16_K(MODE_FOLD);
-    else if (mode == MODE_AUX) MADI_LAUNCH_BF16_K(MODE_AUX);
-    else MADI_LAUNCH_BF16_K(MODE_FREE);
+#define MADI_LAUNCH_BF16_ALL()                                                                            \
+    do {                                                                                                  \
+        if (mode == MODE_FOLD) MADI_LAUNCH_BF16_K(MODE_FOLD);                                             \
+        else if (mode == MODE_AUX) MADI_LAUNCH_BF16_K(MODE_AUX);                                          \
+        else MADI_LAUNCH_BF16_K(MODE_FREE);                                                               \
+    } while (0)
+    // Fixed S0: a probe launch (first step of every voxel
+    // tile) bounds each row's k-th best, the step counts cut each voxel tile's
+    // scan where the principal-axis bound rules out every later tile, and the
+    // main launch starts every row at its bound.  Neither changes a result.
+    const bool full_scan = (d->flags & MADI_MATCH_FLAG_FULL_SCAN) != 0;
+    if (full_scan) P.lmax = nullptr;
+    if (!free_s0 && !full_scan) {
+        e = cudaMemsetAsync(rowout, 0xFF, (size_t)n_vtiles * TILE_M * sizeof(float2), s);
+        if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");
+        P.probe = 1;
+        P.row_out = rowout;
+        MADI_LAUNCH_BF16_ALL();
+        vt_steps_kernel<<<blocks_for(n_vtiles * 32, 256), 256, 0, s>>>(rowout, vkey, vperm, n_vox, n_vtiles, tlo, thi,
+                                                                       order, n_tiles, lmax, vsteps);
+        P.probe = 0;
+        P.row_out = nullptr;
+        P.vt_steps = vsteps;
+        P.row_thr = rowout;
+    }
+    // rows of CTAs that give up on a bounded wait keep no candidates (-1)
+    e = cudaMemsetAsync(P.cand, 0xFF, (size_t)n_vox * EPI_WG * d->topk * sizeof(int32_t), s);
+    if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");
+    MADI_LAUNCH_BF16_ALL();
+#undef MADI_LAUNCH_BF16_ALL
+#define MADI_RESCORE(KK, FR)                                                                              \
+    do {                                                                                                  \
+        if (F <= 24) rescore_kernel<KK, FR, 6><<<blocks_for(2 * n_vox, 256), 256, 0, s>>>(P);             \
+        else rescore_kernel<KK, FR, KPAD / 4><<<blocks_for(2 * n_vox, 256), 256, 0, s>>>(P);             \
+    } while (0)
+#define MADI_RESCORE_K(FR)                                                                                \
+    do {                                                                                                  \
+        if (d->topk == 8) MADI_RESCORE(8, FR);                                                            \
+        else if (d->topk == 16) MADI_RESCORE(16, FR);                                                     \
+        else MADI_RESCORE(32, FR);                                                                        \
+    } while (0)
+    if (free_s0) MADI_RESCORE_K(true);
+    else MADI_RESCORE_K(false);
+#undef MADI_RESCORE_K
+#undef MADI_RESCORE
 #undef MADI_LAUNCH_BF16_K
 #undef MADI_LAUNCH_BF16
     e = cudaGetLastError();

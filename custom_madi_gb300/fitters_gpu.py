@@ -58,7 +58,9 @@ def match_device(measured, lib_mat, *, free_s0: bool = False, precision: str = "
     ``check=True`` waits for the result and raises if the scan could not
     finish (see ``MatchOutput.check``); ``check=False`` returns as soon as the
     work is enqueued on ``stream`` and the caller calls ``.check()`` later.
-    ``flags`` is for tests (MADI_MATCH_FLAG_TEST_STALL).
+    ``flags``: MADI_MATCH_FLAG_FULL_SCAN (BF16 fixed S0 without the
+    principal-axis scan cut; same result up to BF16 score ties at the k-th
+    place) or, for tests, MADI_MATCH_FLAG_TEST_STALL.
     """
     if not HAS_CUDA:
         raise RuntimeError("CUDA is unavailable: the library match runs on a CUDA device only")

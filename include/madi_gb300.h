@@ -274,6 +274,13 @@ enum { MADI_MATCH_FP32 = 0, MADI_MATCH_BF16 = 1 };
  *       smaller rounding than the uncentred form).
  * BF16: tcgen05 BF16 x BF16 -> FP32 (TMEM) scores, a per-voxel top-k (k of 8,
  *       16, 32) candidate list, then an fp32 rescore of the k candidates.
+ *       Fixed S0 (library <= 32768 entries): a first launch over each voxel
+ *       tile's nearest library tile pair bounds every voxel's k-th best BF16
+ *       residual; each voxel tile then scans only the library tiles that the
+ *       principal-axis bound (|m - L| >= |(m - L).pc|, widened by the BF16
+ *       rounding of both vectors) leaves possible.  The cut changes the top-k
+ *       set only in the choice among entries tied in BF16 score at the k-th
+ *       place.
  * measured: device fp32 [n_vox][n_feat]; lib: device fp32 [n_lib][n_feat].
  * scratch: 256-byte aligned device buffer of madi_match_scratch_bytes(...)
  * bytes (contents need no initialisation; FP32 free S0 ignores it).
@@ -299,6 +306,9 @@ typedef struct madi_match_desc {
  * copies and MMAs, frees TMEM, leaves its rows at the caller's fill value) and
  * madi_match_wait reports MADI_ERR_TIMEOUT.  Nothing faults or hangs. */
 #define MADI_MATCH_FLAG_TEST_STALL 1
+/* BF16 fixed S0: scan every library tile for every voxel (no principal-axis
+ * cut); the result is the same up to BF16 score ties at the k-th place. */
+#define MADI_MATCH_FLAG_FULL_SCAN 2
 
 int64_t madi_match_scratch_bytes(int64_t n_vox, int32_t n_lib, int32_t n_feat, int32_t precision,
                                  int32_t topk);

@@ -105,6 +105,62 @@ def test_bf16_tiny_library_ragged_voxels(free):
     np.testing.assert_allclose(res.cpu().numpy(), r64, rtol=1e-4, atol=1e-6)
 
 
+@pytest.mark.parametrize("free", [False, True])
+def test_bf16_one_step_library_over_many_voxel_tiles(free):
+    """200 entries = one step (two library tiles) per voxel tile, 3e5 voxels =
+    2,344 voxel tiles, about 15 per CTA: the two epilogue halves hand over per
+    voxel tile far faster than in a long scan, and every result must still be
+    the fp64 best (status checked)."""
+    from custom_madi_gb300 import workloads as WL
+    from custom_madi_gb300.fitters_gpu import match_device
+    from oracle import oracle as O
+    lib, _ = WL.match_library(n_lib=200)
+    vox, _ = WL.rician_voxels(lib, n_vox=300_000, seed=3)
+    if free:
+        vox = vox * np.random.default_rng(2).uniform(0.5, 2.0, (len(vox), 1))
+    vox, lib = vox.astype(np.float32), lib.astype(np.float32)
+    for k in (8, 32):
+        idx, res, _ = match_device(vox, lib, precision="bf16", topk=k, free_s0=free)
+        idx = idx.cpu().numpy()
+        sub = slice(0, 300_000, 7)
+        if free:
+            i64, _, _ = O.match_free(vox[sub].astype(np.float64), lib.astype(np.float64))
+        else:
+            i64, _ = O.match_fixed(vox[sub].astype(np.float64), lib.astype(np.float64))
+        assert np.all(idx >= 0)
+        assert np.mean(idx[sub] == i64) >= 0.999, (k, np.mean(idx[sub] == i64))
+
+
+def test_bf16_scan_cut_changes_no_result():
+    """Fixed S0: the principal-axis scan cut against the full scan
+    (MADI_MATCH_FLAG_FULL_SCAN) on 2e5 Rician voxels of the 20,000-entry
+    library, all columns and the 2-Delta subset.  Entries whose BF16 rows round
+    to the same vector tie in BF16 score, and which of them holds the k-th place
+    depends on the order the candidates arrive in; only there may the two runs
+    differ, and then the two fp32 residuals lie within the BF16 rounding bound
+    2 u (|m - mu| + max |L - mu|) of each other (u = 2^-8)."""
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300 import workloads as WL
+    from custom_madi_gb300.fitters_gpu import match_device
+    lib, _ = WL.match_library(n_lib=20_000)
+    vox, _ = WL.rician_voxels(lib, n_vox=200_000, seed=8)
+    for cols in (None, WL.two_delta_columns()):
+        v = (vox if cols is None else vox[:, cols]).astype(np.float32)
+        lm = (lib if cols is None else lib[:, cols]).astype(np.float32)
+        mu = lm.astype(np.float64).mean(axis=0)
+        e = 2.0 ** -8 * (np.linalg.norm(v - mu, axis=1) + np.linalg.norm(lm - mu, axis=1).max())
+        for k in (8, 32):
+            ia, ra, _ = match_device(v, lm, precision="bf16", topk=k)
+            ib, rb, _ = match_device(v, lm, precision="bf16", topk=k, flags=N.MADI_MATCH_FLAG_FULL_SCAN)
+            ia, ib, ra, rb = ia.cpu().numpy(), ib.cpu().numpy(), ra.cpu().numpy(), rb.cpu().numpy()
+            d = ia != ib
+            print(f"columns {v.shape[1]} top-{k}: {int(d.sum())} of {len(d)} voxels differ")
+            assert d.mean() <= 1e-4, (cols is None, k, d.mean())
+            gap = np.abs(np.sqrt(np.maximum(ra[d], 0)) - np.sqrt(np.maximum(rb[d], 0)))
+            assert np.all(gap <= 2.0 * e[d] + 1e-6), (cols is None, k)
+            assert np.array_equal(ra[~d], rb[~d])
+
+
 def test_bf16_free_s0_top32_on_rician_voxels():
     """Free S0: BF16 + FP32 rescoring of the top 32 picks the FP64 best index on
     >= 99.9 % of scaled Rician voxels.  (The fp32 scan scores -(m.r)^2/|r|^2, a
