@@ -26,8 +26,16 @@
 // memory, bit masks mark those under the row's current k-th best, and only the
 // marked ones are appended to the row's candidate buffer.  When any lane's
 // buffer would overflow, the warp folds all buffers into the sorted register
-// top-k with bitonic networks.  Each warpgroup rescores its k candidates in
-// fp32 from the fp32 data; the two results are combined (lowest index on ties).
+// top-k with bitonic networks.  At the end of a voxel tile each half writes its
+// candidates (those under the other half's k-th best); rescore_kernel scores
+// them in fp32 from the fp32 data (lowest index on ties).
+//
+// Scan cut (fixed S0): library and voxels are ordered along the library's
+// principal axis, and each voxel tile visits the library tiles nearest its key
+// first.  After a tile's first step, the k-th best of each row over those 256
+// entries bounds its final k-th best; with the BF16 rounding bound, that and
+// |m - L| >= |(m - L).pc| rule out every library tile past a point of the scan
+// order, so the tile's scan stops there (first_step_bounds, steplb_kernel).
 #include <cstdint>
 #include <cuda_bf16.h>
 #include "madi_device.cuh"
@@ -66,6 +74,7 @@ constexpr uint32_t STALL_POLLS = 64;            // the test-only stalled wait (M
 // ran out (every issued copy and MMA then drained), 2 the drain ran out too.
 constexpr int ERR_TIMEOUT = 1;
 constexpr float U_BF16 = 0.00390625f;           // BF16 round-to-nearest: |bf16(x) - x| <= 2^-8 |x|
+constexpr int SLB_CHUNKS = 4;                   // step bounds prefetched per voxel tile (x 32 steps)
 constexpr int ERR_DRAIN = 2;
 
 enum { MODE_FOLD = 0, MODE_AUX = 1, MODE_FREE = 2 };
@@ -471,54 +480,6 @@ __global__ void vox_scatter_kernel(const uint8_t* vb, const uint16_t* vrank, con
     vperm[base[b] + offs[(size_t)b * nblk + blk] + vrank[v]] = (int32_t)v;
 }
 
-// Steps of each voxel tile (fixed S0, after the probe launch).  Every entry j
-// of library tile o has |m~ - L~_j| >= |k(m) - k(L_j)| - u (|m - mu| + |L_j - mu|)
-// (k the principal-axis key, u the BF16 unit roundoff), and for every row of
-// the voxel tile |k(m) - k(L_j)| >= d(o) - W, with d(o) the distance of the
-// tile's key range from the voxel tile's median key and W the rows' largest
-// distance from it.  A tile whose bound exceeds every row's residual bound
-// (the probe's k-th best over the first step, plus u |m - mu|, plus u max|L - mu|)
-// holds no entry that could enter a row's top-k, so the scan keeps the shortest
-// prefix of the order holding every tile that might.  One warp per voxel tile.
-__global__ void vt_steps_kernel(const float2* row_out, const float* vkey, const int32_t* vperm, int64_t n_vox,
-                                int64_t n_vtiles, const float* tlo, const float* thi, const uint16_t* order,
-                                int n_tiles, const float* lmax, uint16_t* steps) {
-    const int64_t vt = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (vt >= n_vtiles) return;
-    const float kmed = vkey[vperm[min(vt * TILE_M + TILE_M / 2, n_vox - 1)]];
-    float W = 0.f, B = 0.f;
-    for (int r = lane; r < TILE_M; r += 32) {
-        const int64_t pos = vt * TILE_M + r;
-        if (pos >= n_vox) break;
-        W = fmaxf(W, fabsf(vkey[vperm[pos]] - kmed));
-        const float b = row_out[pos].y;
-        B = fmaxf(B, b < 3.0e38f ? b : 3.0e38f);     // NaN (no probe result) -> no bound
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        W = fmaxf(W, __shfl_xor_sync(0xffffffffu, W, o));
-        B = fmaxf(B, __shfl_xor_sync(0xffffffffu, B, o));
-    }
-    B += U_BF16 * lmax[0];
-    const float slack = 1e-4f * (1.f + fabsf(kmed) + W);      // fp32 keys and |pc| = 1 to ~1e-6
-    int need = 0;                                   // scan positions [0, need) may hold a candidate
-    for (int base = 0; base < n_tiles; base += 32) {
-        const int i = base + lane;
-        bool keep = false;
-        if (i < n_tiles) {
-            const int o = order[vt * n_tiles + i];
-            const float d = fmaxf(0.f, fmaxf(tlo[o] - kmed, kmed - thi[o]));
-            keep = !((d - W) * (1.f - 1e-5f) - slack > B);
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (m) need = base + 32 - __clz(m);
-    }
-    if (lane == 0) {
-        const int full = (n_tiles + PAIR - 1) / PAIR;
-        steps[vt] = (uint16_t)max(1, min(full, (need + PAIR - 1) / PAIR));
-    }
-}
-
 // Scan order of the library tiles for each voxel tile: the tile holding the
 // voxel tile's median key first, then outward by key distance.
 __global__ void order_kernel(const float* vkey, const int32_t* vperm, int64_t n_vox, int64_t n_vtiles,
@@ -654,10 +615,14 @@ MADI_DEV void append_pass(uint32_t& ma, int oa, uint32_t& mb, int ob, float2*& w
 //   acce[a]             : the eight epilogue warps are done with accumulator a
 //   afull               : a voxel tile (A operand, two buffers) is written
 //                         (warpgroup 0, during the previous voxel tile's first step)
-//   lfull, lempty       : probe launch, end of a voxel tile: warpgroup 1's
-//                         top-k is in its buffer slots / warpgroup 0 has read
-//                         it (warpgroup 1 waits for that before going on, so
-//                         lfull never completes two phases ahead of its waiter)
+//   lfull, lempty       : after a voxel tile's first step (scan cut): warpgroup
+//                         1's top-k is in its stage slots / warpgroup 0 has read
+//                         it and published the tile's step count and row bounds
+//                         (warpgroup 1 waits for that before going on, so lfull
+//                         never completes two phases ahead of its waiter)
+//   rfull               : warpgroup 0's four partial maxima are written
+//   vready              : the voxel tile's step count is written (warpgroup 0,
+//                         warp 0; waited by the producer and warpgroup 0)
 // Tile sequence g runs over (voxel tile of this CTA, library tile); stage
 // g % STAGES, accumulator g % ACCS.  The k-th completion of a barrier is
 // waited with parity k & 1.
@@ -674,11 +639,10 @@ struct Plan {
     const int32_t* lperm;               // library scan position -> caller's library rows
     const float* lrows;                 // fp32 library rows in scan order, KPAD floats each
     const uint16_t* order;              // [voxel tile][scan position] -> library tile
-    const uint16_t* vt_steps;           // steps of each voxel tile (a prefix of its scan); null = all
-    const float2* row_thr;              // per scan row: (k-th best score bound, -) from the probe; or null
-    float2* row_out;                    // probe: per scan row (k-th best score bound, residual bound)
+    const float* steplb;                // [voxel tile][step] lower bound on |m~ - L~| - u |m - mu| - u |L - mu|
+    const float2* rownorm;              // [scan row] (|m~|^2 of the BF16 row, |m - mu|)
     const float* lmax;                  // max over the library of |L - mu| (fixed S0), device scalar
-    int probe;                          // 1: first step of every voxel tile only, write row_out, no candidates
+    int cut;                            // 1: cut each voxel tile's scan after its first step (fixed S0)
     int32_t* cand;                      // [scan row][half][k] candidate scan positions, -1 terminated
     int32_t* best_idx;
     float* best_resid;
@@ -699,8 +663,13 @@ struct Smem {
     uint64_t acce[ACCS];
     int lt_stage[STAGES][PAIR];         // library tiles held by each stage (producer only)
     uint64_t afull;
+    float thr0[TILE_M];                 // row bounds from the first step (warpgroup 0 -> 1)
+    float red[4][2];                    // warpgroup 0 partial maxima of the residual bound
+    int vsteps[2];                      // steps of the current voxel tiles (by parity)
     uint64_t lfull;
     uint64_t lempty;
+    uint64_t rfull;
+    uint64_t vready;
     uint64_t drain;
     uint64_t never;                     // no thread ever arrives (the test-only stalled wait)
     int64_t n_loaded, n_issued;         // producer: steps whose copies / MMAs were issued
@@ -709,19 +678,6 @@ struct Smem {
 };
 
 MADI_DEV int err_flag_read(const Smem& S) { return *reinterpret_cast<const volatile int*>(&S.err); }
-
-// |m~|^2 of the BF16 row the MMA sees (m~ = bf16(m - mu), as write_voxel_tile
-// rounds it) and |m - mu|^2 in fp32, for the fixed-S0 bounds.
-MADI_DEV void row_norms(const Plan& P, int64_t row, float& mh2, float& mn2) {
-    mh2 = 0.f;
-    mn2 = 0.f;
-    for (int k = 0; k < P.F; ++k) {
-        const float x = P.meas[row * P.F + k] - __ldg(P.mu + k);
-        const float xb = __bfloat162float(__float2bfloat16_rn(x));
-        mh2 = fmaf(xb, xb, mh2);
-        mn2 = fmaf(x, x, mn2);
-    }
-}
 
 // Voxel tile -> BF16 canonical A rows (warpgroup 0, each thread its own row),
 // then hand the tile to the async proxy and signal the producer.
@@ -747,11 +703,70 @@ MADI_DEV void write_voxel_tile(Smem& S, const Plan& P, int64_t vt, int buf, int 
     if (lane == 0) mbar_arrive(&S.afull);
 }
 
-// Steps (library tile pairs, a prefix of the scan order) of voxel tile vt.
-MADI_DEV int vtile_steps(const Plan& P, int64_t vt) {
-    const int full = (P.n_tiles + PAIR - 1) / PAIR;
-    if (P.probe) return 1;
-    return P.vt_steps ? (int)P.vt_steps[vt] : full;
+// Steps (library tile pairs) of a whole scan; with the scan cut and more than
+// two steps, a voxel tile's count is known only after its first step (at
+// least two steps are always scanned).
+MADI_DEV int full_steps(const Plan& P) { return (P.n_tiles + PAIR - 1) / PAIR; }
+MADI_DEV bool dynamic_steps(const Plan& P) { return P.cut && full_steps(P) > 2; }
+
+// Scan cut bounds (fixed S0), one warp per voxel tile.  Every entry j of
+// library tile o has |m~ - L~_j| >= |k(m) - k(L_j)| - u (|m - mu| + |L_j - mu|)
+// (k the principal-axis key, u the BF16 unit roundoff), and for every row of
+// the voxel tile |k(m) - k(L_j)| >= d(o) - W, with d(o) the distance of the
+// tile's key range from the voxel tile's median key and W the rows' largest
+// distance from it.  steplb[vt][s] is the smallest of these bounds (less
+// fp32 slack) over scan positions 2s and later, so it does not decrease with
+// s: a step whose steplb exceeds B, every row's residual bound (from its k-th
+// best over the first step) plus u |m - mu| plus u max |L - mu|, and all later
+// steps hold no entry that could enter a row's top-k.
+__global__ void steplb_kernel(const float* vkey, const int32_t* vperm, int64_t n_vox, int64_t n_vtiles,
+                              const float* tlo, const float* thi, const uint16_t* order, int n_tiles, float* steplb) {
+    const int64_t vt = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (vt >= n_vtiles) return;
+    const float kmed = vkey[vperm[min(vt * TILE_M + TILE_M / 2, n_vox - 1)]];
+    float W = 0.f;
+    for (int r = lane; r < TILE_M; r += 32) {
+        const int64_t pos = vt * TILE_M + r;
+        if (pos < n_vox) W = fmaxf(W, fabsf(vkey[vperm[pos]] - kmed));
+    }
+    for (int o = 16; o > 0; o >>= 1) W = fmaxf(W, __shfl_xor_sync(0xffffffffu, W, o));
+    const float slack = 1e-4f * (1.f + fabsf(kmed) + W);      // fp32 keys and |pc| = 1 to ~1e-6
+    const int n_steps = (n_tiles + PAIR - 1) / PAIR;
+    float carry = 3.0e38f;                          // minimum over the positions after this chunk
+    for (int base = ((n_tiles - 1) / 32) * 32; base >= 0; base -= 32) {
+        const int i = base + lane;
+        float lb = 3.0e38f;
+        if (i < n_tiles) {
+            const int o = order[vt * n_tiles + i];
+            const float d = fmaxf(0.f, fmaxf(tlo[o] - kmed, kmed - thi[o]));
+            lb = (d - W) * (1.f - 1e-5f) - slack;
+        }
+        // suffix minimum within the chunk (lanes above), then the chunks after it
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_down_sync(0xffffffffu, lb, o);
+            if (lane + o < 32) lb = fminf(lb, y);
+        }
+        lb = fminf(lb, carry);
+        carry = __shfl_sync(0xffffffffu, lb, 0);
+        if (i < n_tiles && (i & 1) == 0) steplb[vt * n_steps + i / 2] = lb;
+    }
+}
+
+// (|m~|^2 of the BF16 row the MMA sees, |m - mu|) of each scan row (fixed S0).
+__global__ void row_norm_kernel(const float* meas, const int32_t* vperm, int64_t n_vox, int F, const float* mu,
+                                float2* rownorm) {
+    const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= n_vox) return;
+    const int64_t row = vperm[pos];
+    float mh2 = 0.f, mn2 = 0.f;
+    for (int k = 0; k < F; ++k) {
+        const float x = meas[row * F + k] - mu[k];
+        const float xb = __bfloat162float(__float2bfloat16_rn(x));
+        mh2 = fmaf(xb, xb, mh2);
+        mn2 = fmaf(x, x, mn2);
+    }
+    rownorm[pos] = make_float2(mh2, sqrtf(mn2));
 }
 
 // Library tile at scan position i of voxel tile vt (the all-padding tile past the end).
@@ -760,14 +775,18 @@ MADI_DEV int scan_tile(const Plan& P, int64_t vt, int i) {
 }
 
 // Lane 0 of the producer warp waits on barriers and issues the copies and
-// MMAs.  The step sequence runs over this CTA's voxel tiles, each for its
-// vtile_steps; step g covers scan positions 2s and 2s + 1 of its voxel tile
-// (an odd tile count is padded with the all-padding tile n_tiles).  The scan
-// order entries of a load are read one load ahead.
+// MMAs.  The step sequence runs over this CTA's voxel tiles; step s of a tile
+// covers scan positions 2s and 2s + 1 of its order (an odd tile count is
+// padded with the all-padding tile n_tiles).  Under the scan cut a tile's
+// step count comes from warpgroup 0 after its first step (vready): each
+// iteration issues its MMA before its loads, so the load that needs the count
+// (the tile's third step, or the next tile's first) waits for it only after
+// the first step's MMA went out.  Scan order entries are read one load ahead.
 template <int MODE>
 MADI_DEV void producer(Smem& S, const Plan& P, int64_t my_vt, uint32_t tmem, int lane) {
     const uint32_t idesc = make_idesc();
     int64_t gl = 0;                                  // steps loaded
+    int64_t g = 0;                                   // steps whose MMAs were issued
     bool ok = true;
     // The stage refilled with step g + LOAD_AHEAD last held step
     // g + LOAD_AHEAD - STAGES <= g - ACCS; the acce wait that precedes the
@@ -775,44 +794,48 @@ MADI_DEV void producer(Smem& S, const Plan& P, int64_t my_vt, uint32_t tmem, int
     // earlier MMAs') completion, so the stage is free without a barrier of its own.
     static_assert(STAGES - LOAD_AHEAD >= ACCS, "a refilled stage must be certified free by the acce wait");
     if (lane == 0) {
-        int64_t total = 0;
-        for (int64_t lv = 0; lv < my_vt; ++lv) total += vtile_steps(P, blockIdx.x + lv * (int64_t)gridDim.x);
-        // load cursor (voxel tile slot, step, steps of that tile) and the next load's tiles
+        const bool dyn = MODE != MODE_FREE && dynamic_steps(P);
+        const int n_first = dyn ? 2 : full_steps(P);    // steps known before a tile's count
+        int st_first[STAGES], st_par[STAGES];        // per stage: first step of its voxel tile, tile parity
+        // load cursor: voxel tile slot, step, steps known so far, whether that is the count
         int64_t l_lv = 0;
-        int l_s = 0, l_n = my_vt > 0 ? vtile_steps(P, blockIdx.x) : 0;
-        int nt0 = 0, nt1 = 0;
-        auto fetch = [&]() {
-            if (l_lv < my_vt) {
-                const int64_t vt = blockIdx.x + l_lv * (int64_t)gridDim.x;
-                nt0 = scan_tile(P, vt, PAIR * l_s);
-                nt1 = scan_tile(P, vt, PAIR * l_s + 1);
-            }
-        };
-        fetch();
-        auto load = [&](int64_t g) {
-            const int st = (int)(g % STAGES);
-            const int lt0 = nt0, lt1 = nt1;
-            if (++l_s == l_n) {
-                l_s = 0;
+        int l_s = 0, l_n = n_first;
+        bool l_final = !dyn;
+        // the load cursor on the next step that exists; false past the last one
+        auto settle = [&]() -> bool {
+            while (l_lv < my_vt) {
+                if (l_s < l_n) return true;
+                if (!l_final) {
+                    if (!mbar_wait(&S.vready, (uint32_t)(l_lv & 1), SPIN_LIMIT)) { ok = false; return false; }
+                    l_n = S.vsteps[l_lv & 1];
+                    l_final = true;
+                    continue;
+                }
                 ++l_lv;
-                l_n = l_lv < my_vt ? vtile_steps(P, blockIdx.x + l_lv * (int64_t)gridDim.x) : 0;
+                l_s = 0;
+                l_n = n_first;
+                l_final = !dyn;
             }
-            fetch();                                 // the next load's tiles, a whole step ahead
+            return false;
+        };
+        auto load = [&](int64_t q) {
+            const int st = (int)(q % STAGES);
+            const int64_t vt = blockIdx.x + l_lv * (int64_t)gridDim.x;
+            const int lt0 = scan_tile(P, vt, PAIR * l_s), lt1 = scan_tile(P, vt, PAIR * l_s + 1);
+            st_first[st] = l_s == 0;
+            st_par[st] = (int)(l_lv & 1);
+            ++l_s;
             S.lt_stage[st][0] = lt0;
             S.lt_stage[st][1] = lt1;
             mbar_expect_tx(&S.full[st], PAIR * B_BYTES);
             bulk_g2s(S.b[st], P.tiles + (size_t)lt0 * B_BYTES, B_BYTES, &S.full[st]);
             bulk_g2s(S.b[st] + B_BYTES, P.tiles + (size_t)lt1 * B_BYTES, B_BYTES, &S.full[st]);
         };
-        for (; gl < total && gl < LOAD_AHEAD; ++gl) load(gl);
-        int64_t g = 0;                               // steps whose MMAs were issued
-        int64_t m_lv = 0;                            // MMA cursor
-        int m_s = 0, m_n = my_vt > 0 ? vtile_steps(P, blockIdx.x) : 0;
-        for (; g < total && ok; ++g) {
+        for (; gl < LOAD_AHEAD && settle(); ++gl) load(gl);
+        while (ok && g < gl) {                       // loads and MMAs go in the same order, one each per step
             const int st = (int)(g % STAGES), acc = (int)(g % ACCS);
             if (g >= ACCS && !mbar_wait(&S.acce[acc], (uint32_t)((g / ACCS - 1) & 1), SPIN_LIMIT)) { ok = false; break; }
-            if (gl < total && gl <= g + LOAD_AHEAD) load(gl++);
-            if (m_s == 0 && !mbar_wait(&S.afull, (uint32_t)(m_lv & 1), SPIN_LIMIT)) { ok = false; break; }
+            if (st_first[st] && !mbar_wait(&S.afull, (uint32_t)st_par[st], SPIN_LIMIT)) { ok = false; break; }
             if (!mbar_wait(&S.full[st], (uint32_t)((g / STAGES) & 1), SPIN_LIMIT)) { ok = false; break; }
             fence_after();
             if (MODE != MODE_FOLD) {
@@ -821,16 +844,21 @@ MADI_DEV void producer(Smem& S, const Plan& P, int64_t my_vt, uint32_t tmem, int
                 bulk_g2s(S.aux[acc][0], P.aux + (size_t)S.lt_stage[st][0] * TILE_N, AUX_BYTES, &S.accf[acc]);
                 bulk_g2s(S.aux[acc][1], P.aux + (size_t)S.lt_stage[st][1] * TILE_N, AUX_BYTES, &S.accf[acc]);
             }
-            const uint32_t a_base = smem_u32(S.a[m_lv & 1]);
+            const uint32_t a_base = smem_u32(S.a[st_par[st]]);
             const uint32_t b_base = smem_u32(S.b[st]);
             const uint32_t d = tmem + (uint32_t)(acc * MMA_N);
             mma_bf16(d, make_sdesc(a_base), make_sdesc(b_base), idesc, 0u);
             mma_bf16(d, make_sdesc(a_base + 2 * LBO), make_sdesc(b_base + 2 * LBO), idesc, 1u);
             mma_commit(&S.accf[acc]);
-            if (++m_s == m_n) {
-                m_s = 0;
-                ++m_lv;
-                m_n = m_lv < my_vt ? vtile_steps(P, blockIdx.x + m_lv * (int64_t)gridDim.x) : 0;
+            ++g;
+            // loads up to step (g - 1) + LOAD_AHEAD: the acce wait above certified
+            // the MMA of the step that last used each refilled stage
+            for (; gl < g + LOAD_AHEAD; ++gl) {
+                // a load that needs a tile's step count waits for it only once
+                // every loaded step's MMA has gone out
+                if (l_lv < my_vt && l_s >= l_n && !l_final && g < gl) break;
+                if (!settle()) break;
+                load(gl);
             }
         }
         S.n_loaded = gl;
@@ -929,6 +957,87 @@ __global__ void __launch_bounds__(256, 2) rescore_kernel(const Plan P) {
     if (FREE && P.best_s0) P.best_s0[row] = bs0;
 }
 
+// Scan cut, after a voxel tile's first step.  Both halves fold their buffers;
+// warpgroup 1 hands its ascending top-k to warpgroup 0 in its stage slots;
+// warpgroup 0 takes each row's k-th best over the step's 256 entries (the
+// union of the two lists) as the row's bound thr0 on its final k-th best and
+// its residual bound sqrt(thr0 + |m~|^2) + u |m - mu|, reduces the residual
+// bounds over the tile, and warp 0 counts the steps whose key lower bound
+// (steplb, prefetched in slb) does not exceed B.  rn is the row's prefetched
+// (|m~|^2, |m - mu|).  Every wait is bounded; false if one ran out.
+template <int K, int MB>
+MADI_DEV bool first_step_bounds(Smem& S, const Plan& P, int64_t lv, bool live, int wg, int r, int warp, int lane,
+                                float (&ks)[K], int (&kj)[K], float& thr, int& cnt, const float2* mybuf,
+                                float4* mystage, float2 rn, const float (&slb)[SLB_CHUNKS], int64_t vt, float& thr0,
+                                int& n_steps) {
+    merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, 3.0e38f);
+    const uint32_t par = (uint32_t)(lv & 1);
+    if (wg == 1) {
+#pragma unroll
+        for (int q = 0; q < K / 4; ++q)
+            mystage[q * EPI_THREADS] = make_float4(ks[4 * q], ks[4 * q + 1], ks[4 * q + 2], ks[4 * q + 3]);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&S.lfull);
+        if (!mbar_wait_warp(&S.lempty, par, lane)) return false;
+        n_steps = S.vsteps[par];
+        thr0 = S.thr0[r];
+        thr = fminf(thr, thr0);
+        return true;
+    }
+    if (!mbar_wait_warp(&S.lfull, par, lane)) return false;
+    // k-th smallest of the union of the two ascending lists: min over i of max(ks[i - 1], other[k - 1 - i])
+    const float* other = reinterpret_cast<const float*>(&S.stage[0][TILE_M + r]);
+    float t = 3.0e38f;
+#pragma unroll
+    for (int i = 0; i <= K; ++i) {
+        const int j = K - 1 - i;
+        const float a = i > 0 ? ks[i - 1] : -3.0e38f;
+        const float b = i < K ? other[(j >> 2) * (EPI_THREADS * 4) + (j & 3)] : -3.0e38f;
+        t = fminf(t, fmaxf(a, b));
+    }
+    const float lm = __ldg(P.lmax);
+    float rb = 0.f;
+    thr0 = 3.0e38f;
+    if (live) {
+        thr0 = t + fmaxf(fabsf(t) * 1e-6f, 1e-12f);
+        const float r2 = t + rn.x + 1e-5f * (1.f + rn.x + lm * lm);
+        rb = sqrtf(fmaxf(r2, 0.f)) * (1.f + 1e-5f) + U_BF16 * rn.y;
+        rb = rb < 3.0e38f ? rb : 3.0e38f;
+    }
+    S.thr0[r] = thr0;
+    thr = fminf(thr, thr0);
+    for (int o = 16; o > 0; o >>= 1) rb = fmaxf(rb, __shfl_xor_sync(0xffffffffu, rb, o));
+    if (lane == 0) {
+        S.red[warp][0] = rb;
+        mbar_arrive(&S.rfull);
+    }
+    if (warp == 0) {
+        if (!mbar_wait_warp(&S.rfull, par, lane)) return false;
+        const float B = fmaxf(fmaxf(S.red[0][0], S.red[1][0]), fmaxf(S.red[2][0], S.red[3][0])) + U_BF16 * lm;
+        const int full = full_steps(P);
+        int count = 0;                               // steplb does not decrease: the steps within B are a prefix
+#pragma unroll
+        for (int c = 0; c < SLB_CHUNKS; ++c)
+            count += __popc(__ballot_sync(0xffffffffu, c * 32 + lane < full && slb[c] <= B));
+        for (int c = SLB_CHUNKS; c * 32 < full; ++c) {  // libraries beyond SLB_CHUNKS * 32 steps
+            const int s2 = c * 32 + lane;
+            count += __popc(__ballot_sync(0xffffffffu, s2 < full && P.steplb[vt * full + s2] <= B));
+        }
+        const int steps = max(2, min(full, count));
+        if (lane == 0) {
+            S.vsteps[par] = steps;
+            mbar_arrive(&S.vready);
+        }
+        n_steps = steps;
+    } else {
+        if (!mbar_wait_warp(&S.vready, par, lane)) return false;
+        n_steps = S.vsteps[par];
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&S.lempty);
+    return true;
+}
+
 template <int K, int MODE>
 __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
     constexpr int MB = K < 16 ? K : 16;             // merge batch
@@ -946,6 +1055,8 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
         mbar_init(&S.afull, 4);
         mbar_init(&S.lfull, 4);
         mbar_init(&S.lempty, 4);
+        mbar_init(&S.rfull, 4);
+        mbar_init(&S.vready, 1);
         mbar_init(&S.drain, 1);
         mbar_init(&S.never, 1);
         S.n_loaded = 0;
@@ -989,19 +1100,29 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
         }
         for (int64_t lv = 0; lv < my_vt && ok; ++lv) {
             const int64_t vt = blockIdx.x + lv * gridDim.x;
-            const int n_steps = vtile_steps(P, vt);
+            const bool dyn = MODE != MODE_FREE && dynamic_steps(P);   // the scan cut is for fixed S0
+            int n_steps = dyn ? 2 : full_steps(P);   // under the scan cut: set after the first step
             const int64_t pos = vt * TILE_M + r;
             float ks[K];
             int kj[K];
 #pragma unroll
             for (int i = 0; i < K; ++i) { ks[i] = 3.0e38f; kj[i] = 0; }
-            // the probe's bound on this row's final k-th best score (no effect when absent)
-            float thr0 = 3.0e38f;
-            if (P.row_thr && pos < P.n_vox) {
-                const float b = P.row_thr[pos].x;
-                thr0 = b < 3.0e38f ? b : 3.0e38f;            // NaN (no probe result) -> no bound
-            }
+            float thr0 = 3.0e38f;                    // bound on the row's final k-th best (after the first step)
             float thr = thr0;
+            // scan cut inputs, loaded now so that their latency hides behind the first step
+            float2 rn = make_float2(0.f, 0.f);
+            float slb[SLB_CHUNKS];
+#pragma unroll
+            for (int c = 0; c < SLB_CHUNKS; ++c) slb[c] = 3.0e38f;
+            if (dyn) {
+                if (pos < P.n_vox) rn = P.rownorm[pos];
+                if (warp == 0) {
+                    const int full = full_steps(P);
+#pragma unroll
+                    for (int c = 0; c < SLB_CHUNKS; ++c)
+                        if (c * 32 + lane < full) slb[c] = P.steplb[vt * full + c * 32 + lane];
+                }
+            }
             float tthr = -0.5f * thr;                // fold mode: key t hits when t > -thr / 2
             int cnt = 0;
             // library tile of this warpgroup at step t (the padding tile past the end)
@@ -1130,47 +1251,21 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
                 fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.acce[acc]);
+                if (dyn && t == 0 && !first_step_bounds<K, MB>(S, P, lv, pos < P.n_vox, wg, r, warp, lane, ks, kj, thr,
+                                                               cnt, mybuf, mystage, rn, slb, vt, thr0, n_steps)) {
+                    S.err = ERR_TIMEOUT;
+                    ok = false;
+                    break;
+                }
+                if (dyn && t == 0) {
+                    tthr = -0.5f * thr;
+                    S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                }
             }
             if (!ok) break;
             merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
             S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
             const int64_t row = pos < P.n_vox ? P.vperm[pos] : -1;
-            if (P.probe) {
-                // The row's k-th best over the step's two tiles bounds its final
-                // k-th best: (score bound, residual bound) for the step counts.
-                // Warpgroup 1 hands its ascending top-k over in its own buffer
-                // slots and waits until warpgroup 0 has read them.
-                if (wg == 1) {
-#pragma unroll
-                    for (int i = 0; i < K; ++i) mybuf_w[i * EPI_THREADS] = make_float2(ks[i], 0.f);
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(&S.lfull);
-                    if (!mbar_wait_warp(&S.lempty, (uint32_t)(lv & 1), lane)) { S.err = ERR_TIMEOUT; ok = false; break; }
-                } else {
-                    if (!mbar_wait_warp(&S.lfull, (uint32_t)(lv & 1), lane)) { S.err = ERR_TIMEOUT; ok = false; break; }
-                    // k-th smallest of the union of the two ascending lists:
-                    // min over i of max(ks[i - 1], other[k - 1 - i])
-                    const float2* other = &S.buf[0][TILE_M + r];
-                    float t = 3.0e38f;
-#pragma unroll
-                    for (int i = 0; i <= K; ++i) {
-                        const float a = i > 0 ? ks[i - 1] : -3.0e38f;
-                        const float b = i < K ? other[(K - 1 - i) * EPI_THREADS].x : -3.0e38f;
-                        t = fminf(t, fmaxf(a, b));
-                    }
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(&S.lempty);
-                    if (row >= 0) {
-                        float mh2, mn2;
-                        row_norms(P, row, mh2, mn2);
-                        const float lm = __ldg(P.lmax);
-                        const float r2 = t + mh2 + 1e-5f * (1.f + mh2 + lm * lm);
-                        const float rb = sqrtf(fmaxf(r2, 0.f)) * (1.f + 1e-5f) + U_BF16 * sqrtf(mn2);
-                        P.row_out[pos] = make_float2(t + fmaxf(fabsf(t) * 1e-6f, 1e-12f), rb);
-                    }
-                }
-                continue;
-            }
             // Candidates above the other half's k-th best cannot be in the row's
             // overall top-k; ks is ascending, so the rest is a prefix of length nv
             // (a stale partner value only keeps more).
@@ -1217,8 +1312,8 @@ namespace {
 // Scratch layout of the BF16 path (every part 256-byte aligned).
 struct Layout {
     int64_t tiles, aux, mu, err, kmu, pc, cov, lkey, lperm, krange, tlo, thi;
-    int64_t lrows, vkey, vb, vrank, cnt, offs, vtot, vperm, order, rowout, vsteps, lmax, cand;
-    int64_t lvb, lvrank, lcnt, loffs, ltot, total;
+    int64_t lrows, vkey, vb, vrank, cnt, offs, vtot, vperm, order, lmax, cand;
+    int64_t lvb, lvrank, lcnt, loffs, ltot, steplb, rownorm, total;
 };
 
 Layout layout(int64_t n_vox, int64_t n_lib, int topk) {
@@ -1250,8 +1345,6 @@ Layout layout(int64_t n_vox, int64_t n_lib, int topk) {
     L.vtot = take(NBUCKET * 4);
     L.vperm = take(n_vox * 4);
     L.order = take(n_vtiles * n_tiles * 2);
-    L.rowout = take(n_vtiles * TILE_M * 8);
-    L.vsteps = take(n_vtiles * 2);
     L.lmax = take(4);
     L.cand = take(n_vox * EPI_WG * topk * 4);
     const int64_t lnblk = (n_lib + VBLK - 1) / VBLK;
@@ -1260,6 +1353,8 @@ Layout layout(int64_t n_vox, int64_t n_lib, int topk) {
     L.lcnt = take(lnblk * NBUCKET * 4);
     L.loffs = take(lnblk * NBUCKET * 4);
     L.ltot = take(NBUCKET * 4);
+    L.steplb = take(n_vtiles * (n_pad / PAIR) * 4);
+    L.rownorm = take(n_vox * 8);
     L.total = off;
     return L;
 }
@@ -1322,8 +1417,6 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     int* err = reinterpret_cast<int*>(at(Ly.err));
 
     float* lmax = reinterpret_cast<float*>(at(Ly.lmax));
-    float2* rowout = reinterpret_cast<float2*>(at(Ly.rowout));
-    uint16_t* vsteps = reinterpret_cast<uint16_t*>(at(Ly.vsteps));
     cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(lmax, 0, sizeof(float), s);
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");
@@ -1378,6 +1471,8 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     P.lperm = lperm;
     P.lrows = reinterpret_cast<const float*>(at(Ly.lrows));
     P.order = order;
+    P.steplb = reinterpret_cast<const float*>(at(Ly.steplb));
+    P.rownorm = reinterpret_cast<const float2*>(at(Ly.rownorm));
     P.lmax = free_s0 ? nullptr : lmax;
     P.cand = reinterpret_cast<int32_t*>(at(Ly.cand));
     P.best_idx = d->best_idx;
@@ -1410,34 +1505,29 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
         else if (mode == MODE_AUX) MADI_LAUNCH_BF16_K(MODE_AUX);                                          \
         else MADI_LAUNCH_BF16_K(MODE_FREE);                                                               \
     } while (0)
-    // Fixed S0: a probe launch (first step of every voxel
-    // tile) bounds each row's k-th best, the step counts cut each voxel tile's
-    // scan where the principal-axis bound rules out every later tile, and the
-    // main launch starts every row at its bound.  Neither changes a result.
-    const bool full_scan = (d->flags & MADI_MATCH_FLAG_FULL_SCAN) != 0;
-    if (full_scan) P.lmax = nullptr;
-    if (!free_s0 && !full_scan) {
-        e = cudaMemsetAsync(rowout, 0xFF, (size_t)n_vtiles * TILE_M * sizeof(float2), s);
-        if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");
-        P.probe = 1;
-        P.row_out = rowout;
-        MADI_LAUNCH_BF16_ALL();
-        vt_steps_kernel<<<blocks_for(n_vtiles * 32, 256), 256, 0, s>>>(rowout, vkey, vperm, n_vox, n_vtiles, tlo, thi,
-                                                                       order, n_tiles, lmax, vsteps);
-        P.probe = 0;
-        P.row_out = nullptr;
-        P.vt_steps = vsteps;
-        P.row_thr = rowout;
+    // Fixed S0: each voxel tile's scan stops where the principal-axis bound
+    // rules out every later library tile (decided after its first step).
+    P.cut = (!free_s0 && !(d->flags & MADI_MATCH_FLAG_FULL_SCAN)) ? 1 : 0;
+    if (P.cut && (n_tiles + PAIR - 1) / PAIR > 2) {
+        steplb_kernel<<<blocks_for(n_vtiles * 32, 256), 256, 0, s>>>(vkey, vperm, n_vox, n_vtiles, tlo, thi, order, n_tiles,
+                                                                     const_cast<float*>(P.steplb));
+        row_norm_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(d->measured, vperm, n_vox, F, mu,
+                                                               const_cast<float2*>(P.rownorm));
     }
     // rows of CTAs that give up on a bounded wait keep no candidates (-1)
     e = cudaMemsetAsync(P.cand, 0xFF, (size_t)n_vox * EPI_WG * d->topk * sizeof(int32_t), s);
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");
     MADI_LAUNCH_BF16_ALL();
 #undef MADI_LAUNCH_BF16_ALL
+    // 16-byte chunks of a library row the rescore reads: ceil(F / 4), rounded up to an instantiated size
 #define MADI_RESCORE(KK, FR)                                                                              \
     do {                                                                                                  \
-        if (F <= 24) rescore_kernel<KK, FR, 6><<<blocks_for(2 * n_vox, 256), 256, 0, s>>>(P);             \
-        else rescore_kernel<KK, FR, KPAD / 4><<<blocks_for(2 * n_vox, 256), 256, 0, s>>>(P);             \
+        const unsigned rb = blocks_for(2 * n_vox, 256);                                                   \
+        if (F <= 8) rescore_kernel<KK, FR, 2><<<rb, 256, 0, s>>>(P);                                      \
+        else if (F <= 12) rescore_kernel<KK, FR, 3><<<rb, 256, 0, s>>>(P);                                \
+        else if (F <= 20) rescore_kernel<KK, FR, 5><<<rb, 256, 0, s>>>(P);                                \
+        else if (F <= 24) rescore_kernel<KK, FR, 6><<<rb, 256, 0, s>>>(P);                                \
+        else rescore_kernel<KK, FR, KPAD / 4><<<rb, 256, 0, s>>>(P);                                      \
     } while (0)
 #define MADI_RESCORE_K(FR)                                                                                \
     do {                                                                                                  \

@@ -106,15 +106,17 @@ def test_bf16_tiny_library_ragged_voxels(free):
 
 
 @pytest.mark.parametrize("free", [False, True])
-def test_bf16_one_step_library_over_many_voxel_tiles(free):
-    """200 entries = one step (two library tiles) per voxel tile, 3e5 voxels =
-    2,344 voxel tiles, about 15 per CTA: the two epilogue halves hand over per
-    voxel tile far faster than in a long scan, and every result must still be
-    the fp64 best (status checked)."""
+@pytest.mark.parametrize("n_lib", [200, 600])
+def test_bf16_short_scans_over_many_voxel_tiles(free, n_lib):
+    """200 entries = one step (two library tiles) per voxel tile, 600 = three
+    steps (the shortest scan whose step count the cut decides after the first
+    step); 3e5 voxels = 2,344 voxel tiles, about 15 per CTA: the hand-overs
+    between the epilogue halves and the producer come far faster than in a long
+    scan, and every result must still be the fp64 best (status checked)."""
     from custom_madi_gb300 import workloads as WL
     from custom_madi_gb300.fitters_gpu import match_device
     from oracle import oracle as O
-    lib, _ = WL.match_library(n_lib=200)
+    lib, _ = WL.match_library(n_lib=n_lib)
     vox, _ = WL.rician_voxels(lib, n_vox=300_000, seed=3)
     if free:
         vox = vox * np.random.default_rng(2).uniform(0.5, 2.0, (len(vox), 1))
