@@ -603,6 +603,107 @@ MADI_DEV void append_pass(uint32_t& ma, int oa, uint32_t& mb, int ob, float2*& w
 }
 
 // ---------------------------------------------------------------------------
+// Packed top-k (fixed S0, scans of at most 2^PK_BITS positions).  A candidate
+// is one 32-bit word: the BF16 half-residual d = |m~ - L~|^2 / 2 = |m~|^2 / 2 - t
+// (t the folded key), clamped to [0, 3e38], with its low PK_BITS mantissa bits
+// replaced by the scan position.  Words order as (d to 2^-8 of itself,
+// position), so a compare-exchange of the sorting networks is an unsigned min
+// and max, and a buffer entry takes 4 bytes.  The quantisation moves only the
+// choice among entries within 2^-8 of each other in d at the k-th place; the
+// fp32 rescore decides among the candidates.
+// ---------------------------------------------------------------------------
+constexpr int PK_BITS = 15;
+constexpr uint32_t PK_MASK = (1u << PK_BITS) - 1u;
+constexpr uint32_t PK_EMPTY = 0xFFFFFFFFu;
+// packed entries per thread: the whole buffer at top-32; at smaller k the
+// threshold has to tighten sooner, so the buffer folds as often as the float one
+template <int K>
+__host__ __device__ constexpr int cap_pk() { return K >= 32 ? 2 * CAP : CAP; }
+
+MADI_DEV uint32_t pk_word(float d, int pos) {
+    const float dd = d > 0.f ? fminf(d, 3.0e38f) : (d == d ? 0.f : 3.0e38f);   // NaN sorts last
+    return (__float_as_uint(dd) & ~PK_MASK) | (uint32_t)pos;
+}
+// Folded-key threshold t > tthr equivalent to "d below the top of w's quantum".
+MADI_DEV float pk_tthr(uint32_t w, float hm2) {
+    return w >= 0x7F800000u ? -3.0e38f : hm2 - __uint_as_float(w | PK_MASK);
+}
+
+template <int K>
+MADI_DEV void bitonic_sort_u(uint32_t (&a)[K]) {
+#pragma unroll
+    for (int k = 2; k <= K; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+            for (int i = 0; i < K; ++i) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint32_t x = a[i], y = a[l];
+                    const bool up = (i & k) == 0;
+                    a[i] = up ? min(x, y) : max(x, y);
+                    a[l] = up ? max(x, y) : min(x, y);
+                }
+            }
+}
+
+template <int K>
+MADI_DEV void bitonic_clean_u(uint32_t (&a)[K]) {
+#pragma unroll
+    for (int j = K >> 1; j > 0; j >>= 1)
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+            const int l = i ^ j;
+            if (l > i) {
+                const uint32_t x = a[i], y = a[l];
+                a[i] = min(x, y);
+                a[l] = max(x, y);
+            }
+        }
+}
+
+// Packed merge_buffer: folds this thread's buffered words into ks, MB at a time.
+template <int K, int MB>
+MADI_DEV void merge_buffer_u(uint32_t (&ks)[K], uint32_t& thr, int& cnt, const uint32_t* buf, uint32_t thr0) {
+    const int cmax = __reduce_max_sync(0xffffffffu, cnt);
+#pragma unroll 1
+    for (int base = 0; base < cmax; base += MB) {
+        uint32_t b[MB];
+#pragma unroll
+        for (int i = 0; i < MB; ++i) b[i] = base + i < cnt ? buf[(base + i) * EPI_THREADS] : PK_EMPTY;
+        bitonic_sort_u<MB>(b);
+#pragma unroll
+        for (int i = K - MB; i < K; ++i) ks[i] = min(ks[i], b[K - 1 - i]);
+        bitonic_clean_u<K>(ks);
+    }
+    cnt = 0;
+    thr = min(ks[K - 1], thr0);
+}
+
+// Packed append pass (see append_pass): staged keys are folded keys t.
+MADI_DEV void append_pass_u(uint32_t& ma, int oa, uint32_t& mb, int ob, uint32_t*& wp, const float* stage_f, int jc,
+                            float hm2) {
+    int ix[8];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        ix[u] = ma ? __ffs(ma) - 1 + oa : -1;
+        ma &= ma - 1u;
+        ix[u + 4] = mb ? __ffs(mb) - 1 + ob : -1;
+        mb &= mb - 1u;
+    }
+    float kv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) kv[u] = ix[u] >= 0 ? stage_f[(ix[u] >> 2) * (EPI_THREADS * 4) + (ix[u] & 3)] : 0.f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        if (ix[u] >= 0) {
+            *wp = pk_word(hm2 - kv[u], jc + ix[u]);
+            wp += EPI_THREADS;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Main kernel: warps 0-7 are the epilogue (warpgroup h = warp / 4 takes tile
 // h of every step, accumulator columns [128h, 128h + 128), in two 64-column
 // passes; thread tid % 128 = voxel row = TMEM lane), lane 0 of warp 8 is the
@@ -623,6 +724,10 @@ MADI_DEV void append_pass(uint32_t& ma, int oa, uint32_t& mb, int ob, float2*& w
 //   rfull               : warpgroup 0's four partial maxima are written
 //   vready              : the voxel tile's step count is written (warpgroup 0,
 //                         warp 0; waited by the producer and warpgroup 0)
+//   efull, eempty       : packed top-k, end of a voxel tile: warpgroup 1's
+//                         final list is in its stage slots / warpgroup 0 has
+//                         published each row's union k-th word (warpgroup 1
+//                         waits for it, so efull never runs two phases ahead)
 // Tile sequence g runs over (voxel tile of this CTA, library tile); stage
 // g % STAGES, accumulator g % ACCS.  The k-th completion of a barrier is
 // waited with parity k & 1.
@@ -664,12 +769,15 @@ struct Smem {
     int lt_stage[STAGES][PAIR];         // library tiles held by each stage (producer only)
     uint64_t afull;
     float thr0[TILE_M];                 // row bounds from the first step (warpgroup 0 -> 1)
+    uint32_t ucut[TILE_M];              // packed top-k: the k-th word of the union of both halves, per row
     float red[4][2];                    // warpgroup 0 partial maxima of the residual bound
     int vsteps[2];                      // steps of the current voxel tiles (by parity)
     uint64_t lfull;
     uint64_t lempty;
     uint64_t rfull;
     uint64_t vready;
+    uint64_t efull;
+    uint64_t eempty;
     uint64_t drain;
     uint64_t never;                     // no thread ever arrives (the test-only stalled wait)
     int64_t n_loaded, n_issued;         // producer: steps whose copies / MMAs were issued
@@ -1038,7 +1146,281 @@ MADI_DEV bool first_step_bounds(Smem& S, const Plan& P, int64_t lv, bool live, i
     return true;
 }
 
+// first_step_bounds for the packed top-k: the union of the two halves' lists
+// is taken on words, the row's bound thr0 is the union's k-th word, and the
+// residual bound is sqrt(2 d) at the top of that word's quantum.
+template <int K, int MB>
+MADI_DEV bool first_step_bounds_pk(Smem& S, const Plan& P, int64_t lv, bool live, int wg, int r, int warp, int lane,
+                                   uint32_t (&ks)[K], uint32_t& thr, int& cnt, const uint32_t* mybuf,
+                                   float4* mystage, float2 rn, const float (&slb)[SLB_CHUNKS], int64_t vt,
+                                   uint32_t& thr0, int& n_steps) {
+    merge_buffer_u<K, MB>(ks, thr, cnt, mybuf, PK_EMPTY);
+    const uint32_t par = (uint32_t)(lv & 1);
+    if (wg == 1) {
+        uint4* st4 = reinterpret_cast<uint4*>(mystage);
+#pragma unroll
+        for (int q = 0; q < K / 4; ++q) st4[q * EPI_THREADS] = make_uint4(ks[4 * q], ks[4 * q + 1], ks[4 * q + 2], ks[4 * q + 3]);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&S.lfull);
+        if (!mbar_wait_warp(&S.lempty, par, lane)) return false;
+        n_steps = S.vsteps[par];
+        thr0 = __float_as_uint(S.thr0[r]);
+        thr = min(thr, thr0);
+        return true;
+    }
+    if (!mbar_wait_warp(&S.lfull, par, lane)) return false;
+    // k-th smallest of the union of the two ascending lists: min over i of max(ks[i - 1], other[k - 1 - i])
+    const uint32_t* other = reinterpret_cast<const uint32_t*>(&S.stage[0][TILE_M + r]);
+    uint32_t t = PK_EMPTY;
+#pragma unroll
+    for (int i = 0; i <= K; ++i) {
+        const int j = K - 1 - i;
+        const uint32_t a = i > 0 ? ks[i - 1] : 0u;
+        const uint32_t b = i < K ? other[(j >> 2) * (EPI_THREADS * 4) + (j & 3)] : 0u;
+        t = min(t, max(a, b));
+    }
+    const float lm = __ldg(P.lmax);
+    float rb = 0.f;
+    thr0 = PK_EMPTY;
+    if (live) {
+        thr0 = t;
+        const float dhi = t >= 0x7F800000u ? 3.0e38f : __uint_as_float(t | PK_MASK);
+        const float r2 = fminf(2.f * dhi, 3.0e38f) + 1e-5f * (1.f + rn.x + lm * lm);
+        rb = sqrtf(r2) * (1.f + 1e-5f) + U_BF16 * rn.y;
+        rb = rb < 3.0e38f ? rb : 3.0e38f;
+    }
+    S.thr0[r] = __uint_as_float(thr0);
+    thr = min(thr, thr0);
+    for (int o = 16; o > 0; o >>= 1) rb = fmaxf(rb, __shfl_xor_sync(0xffffffffu, rb, o));
+    if (lane == 0) {
+        S.red[warp][0] = rb;
+        mbar_arrive(&S.rfull);
+    }
+    if (warp == 0) {
+        if (!mbar_wait_warp(&S.rfull, par, lane)) return false;
+        const float B = fmaxf(fmaxf(S.red[0][0], S.red[1][0]), fmaxf(S.red[2][0], S.red[3][0])) + U_BF16 * lm;
+        const int full = full_steps(P);
+        int count = 0;                               // steplb does not decrease: the steps within B are a prefix
+#pragma unroll
+        for (int c = 0; c < SLB_CHUNKS; ++c)
+            count += __popc(__ballot_sync(0xffffffffu, c * 32 + lane < full && slb[c] <= B));
+        for (int c = SLB_CHUNKS; c * 32 < full; ++c) {
+            const int s2 = c * 32 + lane;
+            count += __popc(__ballot_sync(0xffffffffu, s2 < full && P.steplb[vt * full + s2] <= B));
+        }
+        const int steps = max(2, min(full, count));
+        if (lane == 0) {
+            S.vsteps[par] = steps;
+            mbar_arrive(&S.vready);
+        }
+        n_steps = steps;
+    } else {
+        if (!mbar_wait_warp(&S.vready, par, lane)) return false;
+        n_steps = S.vsteps[par];
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&S.lempty);
+    return true;
+}
+
+// Epilogue warps with the packed top-k (fixed S0, scans of at most 2^PK_BITS
+// positions): the same steps, hand-offs and scan cut as the kernel's float
+// epilogue, on packed words.
 template <int K, int MODE>
+MADI_DEV void epilogue_pk(Smem& S, const Plan& P, int tid, int warp, int lane, int64_t my_vt, uint32_t tmem) {
+    constexpr int MB = K < 16 ? K : 16;
+    static_assert(MODE != MODE_FREE, "the packed top-k is for fixed S0");
+    const int n_tiles = P.n_tiles;
+    const int wg = warp >> 2;                        // column half
+    const int r = tid & (TILE_M - 1);                // voxel row = TMEM lane
+    uint32_t* mybuf = reinterpret_cast<uint32_t*>(&S.buf[0][0]) + tid;
+    float4* mystage = &S.stage[0][tid];
+    const float* mystage_f = reinterpret_cast<const float*>(mystage);
+    int64_t g = 0;
+    bool ok = true;
+    if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, P, blockIdx.x, 0, r, lane);
+    if (P.test_stall && my_vt > 0 && !mbar_wait_warp(&S.never, 0, lane, STALL_POLLS)) {
+        S.err = ERR_TIMEOUT;    // tests only: the wait runs out like any other would
+        ok = false;
+    }
+    for (int64_t lv = 0; lv < my_vt && ok; ++lv) {
+        const int64_t vt = blockIdx.x + lv * gridDim.x;
+        const bool dyn = dynamic_steps(P);
+        int n_steps = dyn ? 2 : full_steps(P);
+        const int64_t pos = vt * TILE_M + r;
+        uint32_t ks[K];
+#pragma unroll
+        for (int i = 0; i < K; ++i) ks[i] = PK_EMPTY;
+        uint32_t thr0 = PK_EMPTY, thr = PK_EMPTY;
+        float2 rn = make_float2(0.f, 0.f);
+        if (pos < P.n_vox) rn = P.rownorm[pos];     // |m~|^2, |m - mu|: loaded now, used from the first pass
+        float slb[SLB_CHUNKS];
+#pragma unroll
+        for (int c = 0; c < SLB_CHUNKS; ++c) slb[c] = 3.0e38f;
+        if (dyn && warp == 0) {
+            const int full = full_steps(P);
+#pragma unroll
+            for (int c = 0; c < SLB_CHUNKS; ++c)
+                if (c * 32 + lane < full) slb[c] = P.steplb[vt * full + c * 32 + lane];
+        }
+        float hm2 = 0.f;                             // |m~|^2 / 2, set once rn has landed
+        float tthr = -3.0e38f;
+        int cnt = 0;
+        auto my_tile = [&](int t) -> int {
+            const int i = PAIR * t + wg;
+            return i < n_tiles ? (int)P.order[vt * n_tiles + i] : n_tiles;
+        };
+        int lt_next = my_tile(0);
+        for (int t = 0; t < n_steps; ++t, ++g) {
+            const int acc = (int)(g % ACCS);
+            const bool got = mbar_wait_warp(&S.accf[acc], (uint32_t)((g / ACCS) & 1), lane) &&
+                             !__any_sync(0xffffffffu, err_flag_read(S) != 0);   // warp-uniform
+            if (!got) { S.err = ERR_TIMEOUT; ok = false; break; }
+            fence_after();
+            if (t == 0) hm2 = 0.5f * rn.x;
+            const int lt = lt_next;
+            if (t + 1 < n_steps) lt_next = my_tile(t + 1);
+            const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(acc * MMA_N + wg * TILE_N);
+#pragma unroll 1
+            for (int c = 0; c < TILE_N; c += WG_COLS) {
+                const uint32_t taddr = tbase + (uint32_t)c;
+                const float* ax = S.aux[acc][wg] + c;
+                const int jb = lt * TILE_N + c;
+                float key[WG_COLS];
+                tmem_ld64(taddr, key);
+                if (MODE == MODE_AUX) {              // folded key t = m~.L~ - |L~|^2 / 2
+#pragma unroll
+                    for (int i = 0; i < WG_COLS; i += 4) {
+                        const float4 q = *reinterpret_cast<const float4*>(ax + i);
+                        const float qq[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) key[i + u] = fmaf(-0.5f, qq[u], key[i + u]);
+                    }
+                }
+                uint32_t seeded = 0u;
+                if (t == 0 && c == 0) {
+                    uint32_t sk[K];
+#pragma unroll
+                    for (int i = 0; i < K; ++i) sk[i] = pk_word(hm2 - key[i], jb + i);
+                    bitonic_sort_u<K>(sk);
+#pragma unroll
+                    for (int i = 0; i < K; ++i) ks[i] = sk[i];
+                    thr = min(ks[K - 1], thr0);
+                    tthr = pk_tthr(thr, hm2);
+                    S.thr_pub[wg][r] = make_uint2((uint32_t)vt, thr);
+                    seeded = K >= 32 ? 0xFFFFFFFFu : ((1u << K) - 1u);
+                }
+                const uint2 pp = S.thr_pub[wg ^ 1][r];
+                const float tthr_e = fmaxf(tthr, pp.x == (uint32_t)vt ? pk_tthr(pp.y, hm2) : -3.0e38f);
+                {
+                    float ext[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) ext[i] = key[i];
+#pragma unroll
+                    for (int i = 8; i < WG_COLS; ++i) ext[i & 7] = fmaxf(ext[i & 7], key[i]);
+#pragma unroll
+                    for (int w = 4; w > 0; w >>= 1)
+#pragma unroll
+                        for (int i = 0; i < w; ++i) ext[i] = fmaxf(ext[i], ext[i + w]);
+                    if (!__any_sync(0xffffffffu, ext[0] > tthr_e || seeded)) continue;
+                }
+                uint32_t mk[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+                for (int i = 0; i < WG_COLS; ++i)
+                    if (key[i] > tthr_e) mk[i >> 3] |= 1u << (i & 7);
+                uint32_t m0 = (mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24)) & ~seeded;
+                uint32_t m1 = mk[4] | (mk[5] << 8) | (mk[6] << 16) | (mk[7] << 24);
+                const int nh0 = __popc(m0), nh1 = __popc(m1);
+                if (m0 | m1) {
+#pragma unroll
+                    for (int i = 0; i < WG_COLS; i += 4)
+                        mystage[(i >> 2) * EPI_THREADS] = make_float4(key[i], key[i + 1], key[i + 2], key[i + 3]);
+                }
+                uint32_t* wp = mybuf + cnt * EPI_THREADS;
+                if (!__any_sync(0xffffffffu, cnt + nh0 + nh1 > cap_pk<K>())) {
+                    while (__any_sync(0xffffffffu, (m0 | m1) != 0u)) append_pass_u(m0, 0, m1, 32, wp, mystage_f, jb, hm2);
+                    cnt += nh0 + nh1;
+                } else {
+                    uint32_t none = 0u;
+                    if (__any_sync(0xffffffffu, cnt + nh0 > cap_pk<K>())) {
+                        merge_buffer_u<K, MB>(ks, thr, cnt, mybuf, thr0);
+                        tthr = pk_tthr(thr, hm2);
+                        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, thr);
+                        wp = mybuf;
+                    }
+                    while (__any_sync(0xffffffffu, m0 != 0u)) append_pass_u(m0, 0, none, 0, wp, mystage_f, jb, hm2);
+                    cnt += nh0;
+                    if (__any_sync(0xffffffffu, cnt + nh1 > cap_pk<K>())) {
+                        merge_buffer_u<K, MB>(ks, thr, cnt, mybuf, thr0);
+                        tthr = pk_tthr(thr, hm2);
+                        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, thr);
+                        wp = mybuf;
+                    }
+                    while (__any_sync(0xffffffffu, m1 != 0u)) append_pass_u(m1, 32, none, 0, wp, mystage_f, jb, hm2);
+                    cnt += nh1;
+                }
+            }
+            if (t == 0 && wg == 0 && lv + 1 < my_vt)
+                write_voxel_tile<MODE>(S, P, vt + gridDim.x, (int)((lv + 1) & 1), r, lane);
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.acce[acc]);
+            if (dyn && t == 0) {
+                if (!first_step_bounds_pk<K, MB>(S, P, lv, pos < P.n_vox, wg, r, warp, lane, ks, thr, cnt, mybuf,
+                                                 mystage, rn, slb, vt, thr0, n_steps)) {
+                    S.err = ERR_TIMEOUT;
+                    ok = false;
+                    break;
+                }
+                tthr = pk_tthr(thr, hm2);
+                S.thr_pub[wg][r] = make_uint2((uint32_t)vt, thr);
+            }
+        }
+        if (!ok) break;
+        merge_buffer_u<K, MB>(ks, thr, cnt, mybuf, thr0);
+        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, thr);
+        const int64_t row = pos < P.n_vox ? P.vperm[pos] : -1;
+        // The row's top-k is the k smallest words of the two halves' lists: both
+        // halves keep only words up to the union's k-th word.
+        const uint32_t epar = (uint32_t)(lv & 1);
+        uint32_t cut = PK_EMPTY;
+        if (wg == 1) {
+            uint4* st4 = reinterpret_cast<uint4*>(mystage);
+#pragma unroll
+            for (int q = 0; q < K / 4; ++q) st4[q * EPI_THREADS] = make_uint4(ks[4 * q], ks[4 * q + 1], ks[4 * q + 2], ks[4 * q + 3]);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.efull);
+            if (!mbar_wait_warp(&S.eempty, epar, lane)) { S.err = ERR_TIMEOUT; ok = false; break; }
+            cut = S.ucut[r];
+        } else {
+            if (!mbar_wait_warp(&S.efull, epar, lane)) { S.err = ERR_TIMEOUT; ok = false; break; }
+            const uint32_t* other = reinterpret_cast<const uint32_t*>(&S.stage[0][TILE_M + r]);
+#pragma unroll
+            for (int i = 0; i <= K; ++i) {
+                const int j = K - 1 - i;
+                const uint32_t a = i > 0 ? ks[i - 1] : 0u;
+                const uint32_t b = i < K ? other[(j >> 2) * (EPI_THREADS * 4) + (j & 3)] : 0u;
+                cut = min(cut, max(a, b));
+            }
+            S.ucut[r] = cut;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.eempty);
+        }
+        int nv = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i) nv += (ks[i] < 0x7F800000u && ks[i] <= cut) ? 1 : 0;
+        if (row >= 0) {
+            int4* cp = reinterpret_cast<int4*>(P.cand + (pos * EPI_WG + wg) * K);
+#pragma unroll
+            for (int i = 0; i < K; i += 4)
+                cp[i / 4] = make_int4(i < nv ? (int)(ks[i] & PK_MASK) : -1, i + 1 < nv ? (int)(ks[i + 1] & PK_MASK) : -1,
+                                      i + 2 < nv ? (int)(ks[i + 2] & PK_MASK) : -1,
+                                      i + 3 < nv ? (int)(ks[i + 3] & PK_MASK) : -1);
+        }
+    }
+}
+
+template <int K, int MODE, bool PK>
 __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
     constexpr int MB = K < 16 ? K : 16;             // merge batch
     static_assert(CAP % MB == 0 && CAP >= 32 && CAP >= K, "buffer holds whole merge batches, a chunk and the top-k");
@@ -1057,6 +1439,8 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
         mbar_init(&S.lempty, 4);
         mbar_init(&S.rfull, 4);
         mbar_init(&S.vready, 1);
+        mbar_init(&S.efull, 4);
+        mbar_init(&S.eempty, 4);
         mbar_init(&S.drain, 1);
         mbar_init(&S.never, 1);
         S.n_loaded = 0;
@@ -1084,6 +1468,8 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
 
     if (warp == EPI_WARPS) {
         producer<MODE>(S, P, my_vt, tmem, lane);
+    } else if constexpr (PK) {
+        epilogue_pk<K, MODE>(S, P, tid, warp, lane, my_vt, tmem);
     } else {
         const int wg = warp >> 2;                    // column half
         const int r = tid & (TILE_M - 1);            // voxel row = TMEM lane
@@ -1486,34 +1872,39 @@ madi_status madi_match_bf16(const madi_match_desc* d, cudaStream_t s) {
     const size_t smem = sizeof(Smem);
     // one CTA per SM: it allocates all 512 TMEM columns
     const int grid = (int)std::min<int64_t>(n_vtiles, (int64_t)sms);
-#define MADI_LAUNCH_BF16(KK, MD)                                                                          \
+    // fixed S0 scans of at most 2^PK_BITS positions keep packed one-word candidates
+    const bool packed = mode != MODE_FREE && (int64_t)n_pad * TILE_N <= (int64_t(1) << PK_BITS);
+#define MADI_LAUNCH_BF16(KK, MD, PKV)                                                                     \
     do {                                                                                                  \
-        auto k = match_bf16_kernel<KK, MD>;                                                               \
+        auto k = match_bf16_kernel<KK, MD, PKV>;                                                          \
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);             \
         if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 attribute");                          \
         k<<<grid, THREADS, smem, s>>>(P);                                                                 \
     } while (0)
-#define MADI_LAUNCH_BF16_K(MD)                                                                            \
+#define MADI_LAUNCH_BF16_K(MD, PKV)                                                                       \
     do {                                                                                                  \
-        if (d->topk == 8) MADI_LAUNCH_BF16(8, MD);                                                        \
-        else if (d->topk == 16) MADI_LAUNCH_BF16(16, MD);                                                 \
-        else MADI_LAUNCH_BF16(32, MD);                                                                    \
+        if (d->topk == 8) MADI_LAUNCH_BF16(8, MD, PKV);                                                   \
+        else if (d->topk == 16) MADI_LAUNCH_BF16(16, MD, PKV);                                            \
+        else MADI_LAUNCH_BF16(32, MD, PKV);                                                               \
     } while (0)
 #define MADI_LAUNCH_BF16_ALL()                                                                            \
     do {                                                                                                  \
-        if (mode == MODE_FOLD) MADI_LAUNCH_BF16_K(MODE_FOLD);                                             \
-        else if (mode == MODE_AUX) MADI_LAUNCH_BF16_K(MODE_AUX);                                          \
-        else MADI_LAUNCH_BF16_K(MODE_FREE);                                                               \
+        if (mode == MODE_FOLD && packed) MADI_LAUNCH_BF16_K(MODE_FOLD, true);                             \
+        else if (mode == MODE_FOLD) MADI_LAUNCH_BF16_K(MODE_FOLD, false);                                 \
+        else if (mode == MODE_AUX && packed) MADI_LAUNCH_BF16_K(MODE_AUX, true);                          \
+        else if (mode == MODE_AUX) MADI_LAUNCH_BF16_K(MODE_AUX, false);                                   \
+        else MADI_LAUNCH_BF16_K(MODE_FREE, false);                                                        \
     } while (0)
     // Fixed S0: each voxel tile's scan stops where the principal-axis bound
     // rules out every later library tile (decided after its first step).
     P.cut = (!free_s0 && !(d->flags & MADI_MATCH_FLAG_FULL_SCAN)) ? 1 : 0;
-    if (P.cut && (n_tiles + PAIR - 1) / PAIR > 2) {
+    const bool dyn = P.cut && (n_tiles + PAIR - 1) / PAIR > 2;
+    if (dyn)
         steplb_kernel<<<blocks_for(n_vtiles * 32, 256), 256, 0, s>>>(vkey, vperm, n_vox, n_vtiles, tlo, thi, order, n_tiles,
                                                                      const_cast<float*>(P.steplb));
+    if (dyn || packed)
         row_norm_kernel<<<blocks_for(n_vox, 256), 256, 0, s>>>(d->measured, vperm, n_vox, F, mu,
                                                                const_cast<float2*>(P.rownorm));
-    }
     // rows of CTAs that give up on a bounded wait keep no candidates (-1)
     e = cudaMemsetAsync(P.cand, 0xFF, (size_t)n_vox * EPI_WG * d->topk * sizeof(int32_t), s);
     if (e != cudaSuccess) return host::cuda_fail(e, "match bf16 memset");

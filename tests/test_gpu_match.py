@@ -81,9 +81,14 @@ def test_bf16_top32_rescore_matches_fp32_on_rician_voxels():
     assert agree >= 0.999, agree
     assert np.mean(i16 == i64) >= 0.999
     assert np.mean(i32 == i64) >= 0.999
-    # where the indices differ the residuals are equal to fp32 rounding
+    # where the indices differ, the FP32 best was not among the BF16 top-32: its
+    # residual and the chosen one lie within the BF16 rounding bound
+    # 2 u (|m - mu| + max |L - mu|) of each other (u = 2^-8)
     d = i16 != i32
-    np.testing.assert_allclose(r16.cpu().numpy()[d], r32.cpu().numpy()[d], rtol=1e-5, atol=1e-7)
+    mu = lib.astype(np.float32).astype(np.float64).mean(axis=0)
+    e = 2.0 ** -8 * (np.linalg.norm(vox - mu, axis=1) + np.linalg.norm(lib - mu, axis=1).max())
+    gap = np.abs(np.sqrt(r16.cpu().numpy()[d].astype(np.float64)) - np.sqrt(r32.cpu().numpy()[d].astype(np.float64)))
+    assert np.all(gap <= 2.0 * e[d]), (gap, e[d])
 
 
 @pytest.mark.parametrize("free", [False, True])
