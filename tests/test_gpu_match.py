@@ -241,3 +241,32 @@ def test_bf16_top32_on_the_walker_built_library_agrees_with_fp64():
         print(f"{len(cols)} columns: bf16 vs fp64 {np.mean(i16 == i64):.5f}, fp32 vs fp64 {np.mean(i32 == i64):.5f}")
         assert np.mean(i16 == i64) >= 0.999
         assert np.mean(i32 == i64) >= 0.999
+
+
+def _decay_library(n_lib, n_cols, seed):
+    rng = np.random.default_rng(seed)
+    b = np.linspace(0.0, 3.0, n_cols)
+    d1, d2, f = rng.uniform(0.1, 3.0, n_lib), rng.uniform(0.01, 0.5, n_lib), rng.uniform(0.2, 0.9, n_lib)
+    return (f[:, None] * np.exp(-np.outer(d1, b)) + (1 - f[:, None]) * np.exp(-np.outer(d2, b))).astype(np.float32)
+
+
+@pytest.mark.parametrize("n_lib,n_cols", [(3000, 31), (40_000, 20)])
+def test_bf16_fixed_s0_unfolded_bias_and_large_library(n_lib, n_cols):
+    """31 columns leave no room to fold the bias into the MMA (the per-entry
+    |L~|^2 row path); 40,000 entries exceed the packed candidate's 2^15 scan
+    positions (the (score, index) path).  Both with the scan cut: >= 99.9 % of
+    1e4 noisy voxels pick the fp64 best, and the cut matches the full scan up
+    to BF16 score ties at the k-th place."""
+    from custom_madi_gb300 import _native as N
+    from custom_madi_gb300.fitters_gpu import match_device
+    from oracle import oracle as O
+    lib = _decay_library(n_lib, n_cols, seed=n_cols)
+    rng = np.random.default_rng(7)
+    vox = (lib[rng.integers(0, n_lib, 10_000)] + 0.01 * rng.standard_normal((10_000, n_cols))).astype(np.float32)
+    ia, ra, _ = match_device(vox, lib, precision="bf16", topk=32)
+    ib, rb, _ = match_device(vox, lib, precision="bf16", topk=32, flags=N.MADI_MATCH_FLAG_FULL_SCAN)
+    i64, _ = O.match_fixed(vox.astype(np.float64), lib.astype(np.float64), chunk=2000)
+    ia, ib = ia.cpu().numpy(), ib.cpu().numpy()
+    print(f"{n_lib} x {n_cols}: bf16 vs fp64 {np.mean(ia == i64):.5f}, full scan vs fp64 {np.mean(ib == i64):.5f}")
+    assert np.mean(ia == i64) >= 0.999
+    assert np.mean(ia != ib) <= 1e-3
