@@ -270,3 +270,24 @@ def test_bf16_fixed_s0_unfolded_bias_and_large_library(n_lib, n_cols):
     print(f"{n_lib} x {n_cols}: bf16 vs fp64 {np.mean(ia == i64):.5f}, full scan vs fp64 {np.mean(ib == i64):.5f}")
     assert np.mean(ia == i64) >= 0.999
     assert np.mean(ia != ib) <= 1e-3
+
+
+@pytest.mark.parametrize("n_lib", [32_768, 32_769])
+def test_bf16_top16_at_the_packed_candidate_limit(n_lib):
+    """32,768 entries is the largest library whose scan positions fit the packed
+    candidate word (15 bits); one more entry takes the (score, index) path.
+    Both sides of the limit run at top-16 on a dense library (32k bi-exponential
+    decays, noise 0.01, where BF16 near-ties are common): every voxel gets an
+    index and >= 99 % pick the fp64 best (measured 99.35 % packed, 99.53 %
+    with (score, index) pairs, which rescore a few more candidates)."""
+    from custom_madi_gb300.fitters_gpu import match_device
+    from oracle import oracle as O
+    lib = _decay_library(n_lib, 20, seed=11)
+    rng = np.random.default_rng(3)
+    vox = (lib[rng.integers(0, n_lib, 4000)] + 0.01 * rng.standard_normal((4000, 20))).astype(np.float32)
+    idx, _, _ = match_device(vox, lib, precision="bf16", topk=16)
+    idx = idx.cpu().numpy()
+    i64, _ = O.match_fixed(vox.astype(np.float64), lib.astype(np.float64), chunk=1000)
+    assert np.all(idx >= 0)
+    print(f"{n_lib}: top-16 bf16 vs fp64 {np.mean(idx == i64):.5f}")
+    assert np.mean(idx == i64) >= 0.99
