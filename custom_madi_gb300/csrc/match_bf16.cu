@@ -1065,6 +1065,45 @@ __global__ void __launch_bounds__(256, 2) rescore_kernel(const Plan P) {
     if (FREE && P.best_s0) P.best_s0[row] = bs0;
 }
 
+// Warpgroup 0, after its rows' residual bounds rb: reduce them over the tile
+// (rfull), let warp 0 count the steps whose key lower bound (steplb,
+// prefetched in slb) does not exceed B = max rb + u max|L - mu| and publish
+// the count (vready), then release warpgroup 1 (lempty).  False if a bounded
+// wait ran out.
+MADI_DEV bool publish_steps(Smem& S, const Plan& P, uint32_t par, int warp, int lane, float rb, float lm,
+                            const float (&slb)[SLB_CHUNKS], int64_t vt, int& n_steps) {
+    for (int o = 16; o > 0; o >>= 1) rb = fmaxf(rb, __shfl_xor_sync(0xffffffffu, rb, o));
+    if (lane == 0) {
+        S.red[warp][0] = rb;
+        mbar_arrive(&S.rfull);
+    }
+    if (warp == 0) {
+        if (!mbar_wait_warp(&S.rfull, par, lane)) return false;
+        const float B = fmaxf(fmaxf(S.red[0][0], S.red[1][0]), fmaxf(S.red[2][0], S.red[3][0])) + U_BF16 * lm;
+        const int full = full_steps(P);
+        int count = 0;                               // steplb does not decrease: the steps within B are a prefix
+#pragma unroll
+        for (int c = 0; c < SLB_CHUNKS; ++c)
+            count += __popc(__ballot_sync(0xffffffffu, c * 32 + lane < full && slb[c] <= B));
+        for (int c = SLB_CHUNKS; c * 32 < full; ++c) {  // libraries beyond SLB_CHUNKS * 32 steps
+            const int s2 = c * 32 + lane;
+            count += __popc(__ballot_sync(0xffffffffu, s2 < full && P.steplb[vt * full + s2] <= B));
+        }
+        const int steps = max(2, min(full, count));
+        if (lane == 0) {
+            S.vsteps[par] = steps;
+            mbar_arrive(&S.vready);
+        }
+        n_steps = steps;
+    } else {
+        if (!mbar_wait_warp(&S.vready, par, lane)) return false;
+        n_steps = S.vsteps[par];
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&S.lempty);
+    return true;
+}
+
 // Scan cut, after a voxel tile's first step.  Both halves fold their buffers;
 // warpgroup 1 hands its ascending top-k to warpgroup 0 in its stage slots;
 // warpgroup 0 takes each row's k-th best over the step's 256 entries (the
@@ -1114,36 +1153,7 @@ MADI_DEV bool first_step_bounds(Smem& S, const Plan& P, int64_t lv, bool live, i
     }
     S.thr0[r] = thr0;
     thr = fminf(thr, thr0);
-    for (int o = 16; o > 0; o >>= 1) rb = fmaxf(rb, __shfl_xor_sync(0xffffffffu, rb, o));
-    if (lane == 0) {
-        S.red[warp][0] = rb;
-        mbar_arrive(&S.rfull);
-    }
-    if (warp == 0) {
-        if (!mbar_wait_warp(&S.rfull, par, lane)) return false;
-        const float B = fmaxf(fmaxf(S.red[0][0], S.red[1][0]), fmaxf(S.red[2][0], S.red[3][0])) + U_BF16 * lm;
-        const int full = full_steps(P);
-        int count = 0;                               // steplb does not decrease: the steps within B are a prefix
-#pragma unroll
-        for (int c = 0; c < SLB_CHUNKS; ++c)
-            count += __popc(__ballot_sync(0xffffffffu, c * 32 + lane < full && slb[c] <= B));
-        for (int c = SLB_CHUNKS; c * 32 < full; ++c) {  // libraries beyond SLB_CHUNKS * 32 steps
-            const int s2 = c * 32 + lane;
-            count += __popc(__ballot_sync(0xffffffffu, s2 < full && P.steplb[vt * full + s2] <= B));
-        }
-        const int steps = max(2, min(full, count));
-        if (lane == 0) {
-            S.vsteps[par] = steps;
-            mbar_arrive(&S.vready);
-        }
-        n_steps = steps;
-    } else {
-        if (!mbar_wait_warp(&S.vready, par, lane)) return false;
-        n_steps = S.vsteps[par];
-    }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&S.lempty);
-    return true;
+    return publish_steps(S, P, par, warp, lane, rb, lm, slb, vt, n_steps);
 }
 
 // first_step_bounds for the packed top-k: the union of the two halves' lists
@@ -1191,36 +1201,7 @@ MADI_DEV bool first_step_bounds_pk(Smem& S, const Plan& P, int64_t lv, bool live
     }
     S.thr0[r] = __uint_as_float(thr0);
     thr = min(thr, thr0);
-    for (int o = 16; o > 0; o >>= 1) rb = fmaxf(rb, __shfl_xor_sync(0xffffffffu, rb, o));
-    if (lane == 0) {
-        S.red[warp][0] = rb;
-        mbar_arrive(&S.rfull);
-    }
-    if (warp == 0) {
-        if (!mbar_wait_warp(&S.rfull, par, lane)) return false;
-        const float B = fmaxf(fmaxf(S.red[0][0], S.red[1][0]), fmaxf(S.red[2][0], S.red[3][0])) + U_BF16 * lm;
-        const int full = full_steps(P);
-        int count = 0;                               // steplb does not decrease: the steps within B are a prefix
-#pragma unroll
-        for (int c = 0; c < SLB_CHUNKS; ++c)
-            count += __popc(__ballot_sync(0xffffffffu, c * 32 + lane < full && slb[c] <= B));
-        for (int c = SLB_CHUNKS; c * 32 < full; ++c) {
-            const int s2 = c * 32 + lane;
-            count += __popc(__ballot_sync(0xffffffffu, s2 < full && P.steplb[vt * full + s2] <= B));
-        }
-        const int steps = max(2, min(full, count));
-        if (lane == 0) {
-            S.vsteps[par] = steps;
-            mbar_arrive(&S.vready);
-        }
-        n_steps = steps;
-    } else {
-        if (!mbar_wait_warp(&S.vready, par, lane)) return false;
-        n_steps = S.vsteps[par];
-    }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&S.lempty);
-    return true;
+    return publish_steps(S, P, par, warp, lane, rb, lm, slb, vt, n_steps);
 }
 
 // Epilogue warps with the packed top-k (fixed S0, scans of at most 2^PK_BITS
