@@ -52,6 +52,25 @@ def test_struct_layout_matches_header(tmp_path):
             assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
 
 
+def test_header_constants_match_the_python_mirror():
+    """Every numeric #define of the header that _native mirrors has the same value."""
+    header = (ROOT / "include" / "madi_gb300.h").read_text()
+    defines = {m.group(1): int(m.group(2)) for m in re.finditer(r"^#define\s+(MADI_\w+)\s+(\d+)\b", header, re.M)}
+    mirrored = {k: v for k, v in defines.items() if hasattr(N, k)}
+    assert {"MADI_MATCH_FLAG_TEST_STALL", "MADI_MATCH_FLAG_FULL_SCAN"} <= set(mirrored)
+    for k, v in mirrored.items():
+        assert getattr(N, k) == v, k
+
+
+def test_bf16_match_scratch_holds_the_candidate_lists():
+    """The BF16 scratch grows by two k-entry candidate lists (int32) per voxel."""
+    lib = N.lib()
+    b8 = lib.madi_match_scratch_bytes(100_000, 20_000, 20, N.MADI_MATCH_BF16, 8)
+    b32 = lib.madi_match_scratch_bytes(100_000, 20_000, 20, N.MADI_MATCH_BF16, 32)
+    assert b8 > 0 and b32 - b8 >= 100_000 * 2 * (32 - 8) * 4
+    assert lib.madi_match_scratch_bytes(200_000, 20_000, 20, N.MADI_MATCH_BF16, 32) > b32
+
+
 def test_error_string_and_invalid_arguments():
     lib = N.lib()
     st = lib.madi_kdtree_build(None, 0, None, None, None, None, None)
