@@ -1401,11 +1401,219 @@ MADI_DEV void epilogue_pk(Smem& S, const Plan& P, int tid, int warp, int lane, i
     }
 }
 
-template <int K, int MODE, bool PK>
-__global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
+// Epilogue warps with (score, index) candidates: free S0, and fixed S0 scans
+// beyond 2^PK_BITS positions.  Same steps, hand-offs and scan cut as
+// epilogue_pk; each half's candidates are those under the other half's k-th
+// best.
+template <int K, int MODE>
+MADI_DEV void epilogue_f(Smem& S, const Plan& P, int tid, int warp, int lane, int64_t my_vt, uint32_t tmem) {
     constexpr int MB = K < 16 ? K : 16;             // merge batch
     static_assert(CAP % MB == 0 && CAP >= 32 && CAP >= K, "buffer holds whole merge batches, a chunk and the top-k");
     constexpr bool FREE = MODE == MODE_FREE;
+    const int n_tiles = P.n_tiles;
+    const int wg = warp >> 2;                    // column half
+    const int r = tid & (TILE_M - 1);            // voxel row = TMEM lane
+    const float2* mybuf = &S.buf[0][tid];
+    float2* mybuf_w = &S.buf[0][tid];
+    float4* mystage = &S.stage[0][tid];
+    const float* mystage_f = reinterpret_cast<const float*>(mystage);
+    int64_t g = 0;
+    bool ok = true;
+    if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, P, blockIdx.x, 0, r, lane);
+    if (P.test_stall && my_vt > 0 && !mbar_wait_warp(&S.never, 0, lane, STALL_POLLS)) {
+        S.err = ERR_TIMEOUT;    // tests only: the wait runs out like any other would
+        ok = false;
+    }
+    for (int64_t lv = 0; lv < my_vt && ok; ++lv) {
+        const int64_t vt = blockIdx.x + lv * gridDim.x;
+        const bool dyn = MODE != MODE_FREE && dynamic_steps(P);   // the scan cut is for fixed S0
+        int n_steps = dyn ? 2 : full_steps(P);   // under the scan cut: set after the first step
+        const int64_t pos = vt * TILE_M + r;
+        float ks[K];
+        int kj[K];
+#pragma unroll
+        for (int i = 0; i < K; ++i) { ks[i] = 3.0e38f; kj[i] = 0; }
+        float thr0 = 3.0e38f;                    // bound on the row's final k-th best (after the first step)
+        float thr = thr0;
+        // scan cut inputs, loaded now so that their latency hides behind the first step
+        float2 rn = make_float2(0.f, 0.f);
+        float slb[SLB_CHUNKS];
+#pragma unroll
+        for (int c = 0; c < SLB_CHUNKS; ++c) slb[c] = 3.0e38f;
+        if (dyn) {
+            if (pos < P.n_vox) rn = P.rownorm[pos];
+            if (warp == 0) {
+                const int full = full_steps(P);
+#pragma unroll
+                for (int c = 0; c < SLB_CHUNKS; ++c)
+                    if (c * 32 + lane < full) slb[c] = P.steplb[vt * full + c * 32 + lane];
+            }
+        }
+        float tthr = -0.5f * thr;                // fold mode: key t hits when t > -thr / 2
+        int cnt = 0;
+        // library tile of this warpgroup at step t (the padding tile past the end)
+        auto my_tile = [&](int t) -> int {
+            const int i = PAIR * t + wg;
+            return i < n_tiles ? (int)P.order[vt * n_tiles + i] : n_tiles;
+        };
+        int lt_next = my_tile(0);
+        for (int t = 0; t < n_steps; ++t, ++g) {
+            const int acc = (int)(g % ACCS);
+            const bool got = mbar_wait_warp(&S.accf[acc], (uint32_t)((g / ACCS) & 1), lane) &&
+                             !__any_sync(0xffffffffu, err_flag_read(S) != 0);   // warp-uniform
+            if (!got) { S.err = ERR_TIMEOUT; ok = false; break; }
+            fence_after();
+            const int lt = lt_next;
+            if (t + 1 < n_steps) lt_next = my_tile(t + 1);   // prefetch the next step
+            const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(acc * MMA_N + wg * TILE_N);
+#pragma unroll 1
+            for (int c = 0; c < TILE_N; c += WG_COLS) {
+                const uint32_t taddr = tbase + (uint32_t)c;
+                const float* ax = S.aux[acc][wg] + c;
+                const int jb = lt * TILE_N + c;
+                float key[WG_COLS];
+                tmem_ld64(taddr, key);
+                if (MODE != MODE_FOLD) {
+#pragma unroll
+                    for (int i = 0; i < WG_COLS; i += 4) {
+                        const float4 q = *reinterpret_cast<const float4*>(ax + i);
+                        const float qq[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const float v = key[i + u];
+                            key[i + u] = FREE ? (-v * fabsf(v)) * qq[u] : fmaf(-2.f, v, qq[u]);
+                        }
+                    }
+                }
+                uint32_t seeded = 0u;   // bits of this pass already in ks
+            if (t == 0 && c == 0) {
+                // seed the top-k with the pass's first K keys (the nearest tile):
+                // a finite threshold from the start keeps the early tiles cheap
+                float sk[K];
+                int sj[K];
+#pragma unroll
+                for (int i = 0; i < K; ++i) {
+                    const float sc = MODE == MODE_FOLD ? -2.f * key[i] : key[i];
+                    sk[i] = sc < 3.0e38f ? sc : 3.0e38f;   // padding (inf / NaN) sorts last
+                    sj[i] = jb + i;
+                }
+                bitonic_sort<K>(sk, sj);
+#pragma unroll
+                for (int i = 0; i < K; ++i) { ks[i] = sk[i]; kj[i] = sj[i]; }
+                thr = fminf(ks[K - 1], thr0);
+                tthr = -0.5f * thr;
+                S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                seeded = K >= 32 ? 0xFFFFFFFFu : ((1u << K) - 1u);
+            }
+            // An entry at or above the other half's k-th best of this row
+                // cannot be in the row's overall top-k: filter with the tighter of
+                // the two (a stale read is only looser).
+                const uint2 pp = S.thr_pub[wg ^ 1][r];
+                const float thr_e = fminf(thr, pp.x == (uint32_t)vt ? __uint_as_float(pp.y) : 3.0e38f);
+                const float tthr_e = MODE == MODE_FOLD ? fmaxf(tthr, -0.5f * thr_e) : tthr;
+                // fast path: no lane of the warp holds a candidate in this tile
+                {
+                    float ext[8];   // eight independent running extremes, then a tree
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) ext[i] = key[i];
+#pragma unroll
+                    for (int i = 8; i < WG_COLS; ++i)
+                        ext[i & 7] = MODE == MODE_FOLD ? fmaxf(ext[i & 7], key[i]) : fminf(ext[i & 7], key[i]);
+#pragma unroll
+                    for (int w = 4; w > 0; w >>= 1)
+#pragma unroll
+                        for (int i = 0; i < w; ++i)
+                            ext[i] = MODE == MODE_FOLD ? fmaxf(ext[i], ext[i + w]) : fminf(ext[i], ext[i + w]);
+                    const bool maybe = MODE == MODE_FOLD ? ext[0] > tthr_e : ext[0] < thr_e;
+                    if (!__any_sync(0xffffffffu, maybe || seeded)) continue;   // nothing for this warp here
+                }
+                // eight independent 8-bit masks, then two 32-bit masks
+                uint32_t mk[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+                for (int i = 0; i < WG_COLS; ++i) {
+                    const bool hit = MODE == MODE_FOLD ? key[i] > tthr_e : key[i] < thr_e;
+                    if (hit) mk[i >> 3] |= 1u << (i & 7);
+                }
+                uint32_t m0 = (mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24)) & ~seeded;
+                uint32_t m1 = mk[4] | (mk[5] << 8) | (mk[6] << 16) | (mk[7] << 24);
+                const int nh0 = __popc(m0), nh1 = __popc(m1);
+                if (m0 | m1) {   // stage the keys for the append passes (lanes with hits only)
+#pragma unroll
+                    for (int i = 0; i < WG_COLS; i += 4)
+                        mystage[(i >> 2) * EPI_THREADS] = make_float4(key[i], key[i + 1], key[i + 2], key[i + 3]);
+                }
+                float2* wp = mybuf_w + cnt * EPI_THREADS;
+                if (!__any_sync(0xffffffffu, cnt + nh0 + nh1 > CAP)) {
+                    while (__any_sync(0xffffffffu, (m0 | m1) != 0u)) append_pass<MODE>(m0, 0, m1, 32, wp, mystage_f, jb);
+                    cnt += nh0 + nh1;
+                } else {
+                    // fold before each half as needed, then append it
+                    uint32_t none = 0u;
+                    if (__any_sync(0xffffffffu, cnt + nh0 > CAP)) {
+                        merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
+                        tthr = -0.5f * thr;
+                        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                        wp = mybuf_w;
+                    }
+                    while (__any_sync(0xffffffffu, m0 != 0u)) append_pass<MODE>(m0, 0, none, 0, wp, mystage_f, jb);
+                    cnt += nh0;
+                    if (__any_sync(0xffffffffu, cnt + nh1 > CAP)) {
+                        merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
+                        tthr = -0.5f * thr;
+                        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+                        wp = mybuf_w;
+                    }
+                    while (__any_sync(0xffffffffu, m1 != 0u)) append_pass<MODE>(m1, 32, none, 0, wp, mystage_f, jb);
+                    cnt += nh1;
+                }
+            }
+            // After the first step, the next voxel tile's A goes into the other
+            // buffer: its last reader, the previous voxel tile's MMAs, completed
+            // before this tile's first step did, and the producer has already
+            // waited on this tile's afull phase, so afull never runs two phases
+            // ahead of its waiter.
+            if (t == 0 && wg == 0 && lv + 1 < my_vt)
+                write_voxel_tile<MODE>(S, P, vt + gridDim.x, (int)((lv + 1) & 1), r, lane);
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.acce[acc]);
+            if (dyn && t == 0 && !first_step_bounds<K, MB>(S, P, lv, pos < P.n_vox, wg, r, warp, lane, ks, kj, thr,
+                                                           cnt, mybuf, mystage, rn, slb, vt, thr0, n_steps)) {
+                S.err = ERR_TIMEOUT;
+                ok = false;
+                break;
+            }
+            if (dyn && t == 0) {
+                tthr = -0.5f * thr;
+                S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+            }
+        }
+        if (!ok) break;
+        merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
+        S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
+        const int64_t row = pos < P.n_vox ? P.vperm[pos] : -1;
+        // Candidates above the other half's k-th best cannot be in the row's
+        // overall top-k; ks is ascending, so the rest is a prefix of length nv
+        // (a stale partner value only keeps more).
+        const uint2 pp = S.thr_pub[wg ^ 1][r];
+        const float cut = fminf(3.0e38f, pp.x == (uint32_t)vt ? __uint_as_float(pp.y) : 3.0e38f);
+        int nv = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i) nv += (ks[i] < 3.0e38f && ks[i] <= cut) ? 1 : 0;
+        // candidates (scan positions, ascending BF16 score) for the rescore kernel
+        if (row >= 0) {
+            int4* c = reinterpret_cast<int4*>(P.cand + (pos * EPI_WG + wg) * K);
+#pragma unroll
+            for (int i = 0; i < K; i += 4)
+                c[i / 4] = make_int4(i < nv ? kj[i] : -1, i + 1 < nv ? kj[i + 1] : -1, i + 2 < nv ? kj[i + 2] : -1,
+                                     i + 3 < nv ? kj[i + 3] : -1);
+        }
+    }
+}
+
+template <int K, int MODE, bool PK>
+__global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
+    static_assert(!PK || MODE != MODE_FREE, "packed candidates are for fixed S0");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1444,7 +1652,6 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
     fence_after();
     const uint32_t tmem = S.tmem_base;
     const int64_t n_vtiles = (P.n_vox + TILE_M - 1) / TILE_M;
-    const int n_tiles = P.n_tiles;
     const int64_t my_vt = (int64_t)blockIdx.x < n_vtiles ? (n_vtiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
     if (warp == EPI_WARPS) {
@@ -1452,204 +1659,7 @@ __global__ void __launch_bounds__(THREADS, 1) match_bf16_kernel(const Plan P) {
     } else if constexpr (PK) {
         epilogue_pk<K, MODE>(S, P, tid, warp, lane, my_vt, tmem);
     } else {
-        const int wg = warp >> 2;                    // column half
-        const int r = tid & (TILE_M - 1);            // voxel row = TMEM lane
-        const float2* mybuf = &S.buf[0][tid];
-        float2* mybuf_w = &S.buf[0][tid];
-        float4* mystage = &S.stage[0][tid];
-        const float* mystage_f = reinterpret_cast<const float*>(mystage);
-        int64_t g = 0;
-        bool ok = true;
-        if (wg == 0 && my_vt > 0) write_voxel_tile<MODE>(S, P, blockIdx.x, 0, r, lane);
-        if (P.test_stall && my_vt > 0 && !mbar_wait_warp(&S.never, 0, lane, STALL_POLLS)) {
-            S.err = ERR_TIMEOUT;    // tests only: the wait runs out like any other would
-            ok = false;
-        }
-        for (int64_t lv = 0; lv < my_vt && ok; ++lv) {
-            const int64_t vt = blockIdx.x + lv * gridDim.x;
-            const bool dyn = MODE != MODE_FREE && dynamic_steps(P);   // the scan cut is for fixed S0
-            int n_steps = dyn ? 2 : full_steps(P);   // under the scan cut: set after the first step
-            const int64_t pos = vt * TILE_M + r;
-            float ks[K];
-            int kj[K];
-#pragma unroll
-            for (int i = 0; i < K; ++i) { ks[i] = 3.0e38f; kj[i] = 0; }
-            float thr0 = 3.0e38f;                    // bound on the row's final k-th best (after the first step)
-            float thr = thr0;
-            // scan cut inputs, loaded now so that their latency hides behind the first step
-            float2 rn = make_float2(0.f, 0.f);
-            float slb[SLB_CHUNKS];
-#pragma unroll
-            for (int c = 0; c < SLB_CHUNKS; ++c) slb[c] = 3.0e38f;
-            if (dyn) {
-                if (pos < P.n_vox) rn = P.rownorm[pos];
-                if (warp == 0) {
-                    const int full = full_steps(P);
-#pragma unroll
-                    for (int c = 0; c < SLB_CHUNKS; ++c)
-                        if (c * 32 + lane < full) slb[c] = P.steplb[vt * full + c * 32 + lane];
-                }
-            }
-            float tthr = -0.5f * thr;                // fold mode: key t hits when t > -thr / 2
-            int cnt = 0;
-            // library tile of this warpgroup at step t (the padding tile past the end)
-            auto my_tile = [&](int t) -> int {
-                const int i = PAIR * t + wg;
-                return i < n_tiles ? (int)P.order[vt * n_tiles + i] : n_tiles;
-            };
-            int lt_next = my_tile(0);
-            for (int t = 0; t < n_steps; ++t, ++g) {
-                const int acc = (int)(g % ACCS);
-                const bool got = mbar_wait_warp(&S.accf[acc], (uint32_t)((g / ACCS) & 1), lane) &&
-                                 !__any_sync(0xffffffffu, err_flag_read(S) != 0);   // warp-uniform
-                if (!got) { S.err = ERR_TIMEOUT; ok = false; break; }
-                fence_after();
-                const int lt = lt_next;
-                if (t + 1 < n_steps) lt_next = my_tile(t + 1);   // prefetch the next step
-                const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(acc * MMA_N + wg * TILE_N);
-#pragma unroll 1
-                for (int c = 0; c < TILE_N; c += WG_COLS) {
-                    const uint32_t taddr = tbase + (uint32_t)c;
-                    const float* ax = S.aux[acc][wg] + c;
-                    const int jb = lt * TILE_N + c;
-                    float key[WG_COLS];
-                    tmem_ld64(taddr, key);
-                    if (MODE != MODE_FOLD) {
-#pragma unroll
-                        for (int i = 0; i < WG_COLS; i += 4) {
-                            const float4 q = *reinterpret_cast<const float4*>(ax + i);
-                            const float qq[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                const float v = key[i + u];
-                                key[i + u] = FREE ? (-v * fabsf(v)) * qq[u] : fmaf(-2.f, v, qq[u]);
-                            }
-                        }
-                    }
-                    uint32_t seeded = 0u;   // bits of this pass already in ks
-                if (t == 0 && c == 0) {
-                    // seed the top-k with the pass's first K keys (the nearest tile):
-                    // a finite threshold from the start keeps the early tiles cheap
-                    float sk[K];
-                    int sj[K];
-#pragma unroll
-                    for (int i = 0; i < K; ++i) {
-                        const float sc = MODE == MODE_FOLD ? -2.f * key[i] : key[i];
-                        sk[i] = sc < 3.0e38f ? sc : 3.0e38f;   // padding (inf / NaN) sorts last
-                        sj[i] = jb + i;
-                    }
-                    bitonic_sort<K>(sk, sj);
-#pragma unroll
-                    for (int i = 0; i < K; ++i) { ks[i] = sk[i]; kj[i] = sj[i]; }
-                    thr = fminf(ks[K - 1], thr0);
-                    tthr = -0.5f * thr;
-                    S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
-                    seeded = K >= 32 ? 0xFFFFFFFFu : ((1u << K) - 1u);
-                }
-                // An entry at or above the other half's k-th best of this row
-                    // cannot be in the row's overall top-k: filter with the tighter of
-                    // the two (a stale read is only looser).
-                    const uint2 pp = S.thr_pub[wg ^ 1][r];
-                    const float thr_e = fminf(thr, pp.x == (uint32_t)vt ? __uint_as_float(pp.y) : 3.0e38f);
-                    const float tthr_e = MODE == MODE_FOLD ? fmaxf(tthr, -0.5f * thr_e) : tthr;
-                    // fast path: no lane of the warp holds a candidate in this tile
-                    {
-                        float ext[8];   // eight independent running extremes, then a tree
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) ext[i] = key[i];
-#pragma unroll
-                        for (int i = 8; i < WG_COLS; ++i)
-                            ext[i & 7] = MODE == MODE_FOLD ? fmaxf(ext[i & 7], key[i]) : fminf(ext[i & 7], key[i]);
-#pragma unroll
-                        for (int w = 4; w > 0; w >>= 1)
-#pragma unroll
-                            for (int i = 0; i < w; ++i)
-                                ext[i] = MODE == MODE_FOLD ? fmaxf(ext[i], ext[i + w]) : fminf(ext[i], ext[i + w]);
-                        const bool maybe = MODE == MODE_FOLD ? ext[0] > tthr_e : ext[0] < thr_e;
-                        if (!__any_sync(0xffffffffu, maybe || seeded)) continue;   // nothing for this warp here
-                    }
-                    // eight independent 8-bit masks, then two 32-bit masks
-                    uint32_t mk[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-#pragma unroll
-                    for (int i = 0; i < WG_COLS; ++i) {
-                        const bool hit = MODE == MODE_FOLD ? key[i] > tthr_e : key[i] < thr_e;
-                        if (hit) mk[i >> 3] |= 1u << (i & 7);
-                    }
-                    uint32_t m0 = (mk[0] | (mk[1] << 8) | (mk[2] << 16) | (mk[3] << 24)) & ~seeded;
-                    uint32_t m1 = mk[4] | (mk[5] << 8) | (mk[6] << 16) | (mk[7] << 24);
-                    const int nh0 = __popc(m0), nh1 = __popc(m1);
-                    if (m0 | m1) {   // stage the keys for the append passes (lanes with hits only)
-#pragma unroll
-                        for (int i = 0; i < WG_COLS; i += 4)
-                            mystage[(i >> 2) * EPI_THREADS] = make_float4(key[i], key[i + 1], key[i + 2], key[i + 3]);
-                    }
-                    float2* wp = mybuf_w + cnt * EPI_THREADS;
-                    if (!__any_sync(0xffffffffu, cnt + nh0 + nh1 > CAP)) {
-                        while (__any_sync(0xffffffffu, (m0 | m1) != 0u)) append_pass<MODE>(m0, 0, m1, 32, wp, mystage_f, jb);
-                        cnt += nh0 + nh1;
-                    } else {
-                        // fold before each half as needed, then append it
-                        uint32_t none = 0u;
-                        if (__any_sync(0xffffffffu, cnt + nh0 > CAP)) {
-                            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
-                            tthr = -0.5f * thr;
-                            S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
-                            wp = mybuf_w;
-                        }
-                        while (__any_sync(0xffffffffu, m0 != 0u)) append_pass<MODE>(m0, 0, none, 0, wp, mystage_f, jb);
-                        cnt += nh0;
-                        if (__any_sync(0xffffffffu, cnt + nh1 > CAP)) {
-                            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
-                            tthr = -0.5f * thr;
-                            S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
-                            wp = mybuf_w;
-                        }
-                        while (__any_sync(0xffffffffu, m1 != 0u)) append_pass<MODE>(m1, 32, none, 0, wp, mystage_f, jb);
-                        cnt += nh1;
-                    }
-                }
-                // After the first step, the next voxel tile's A goes into the other
-                // buffer: its last reader, the previous voxel tile's MMAs, completed
-                // before this tile's first step did, and the producer has already
-                // waited on this tile's afull phase, so afull never runs two phases
-                // ahead of its waiter.
-                if (t == 0 && wg == 0 && lv + 1 < my_vt)
-                    write_voxel_tile<MODE>(S, P, vt + gridDim.x, (int)((lv + 1) & 1), r, lane);
-                fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&S.acce[acc]);
-                if (dyn && t == 0 && !first_step_bounds<K, MB>(S, P, lv, pos < P.n_vox, wg, r, warp, lane, ks, kj, thr,
-                                                               cnt, mybuf, mystage, rn, slb, vt, thr0, n_steps)) {
-                    S.err = ERR_TIMEOUT;
-                    ok = false;
-                    break;
-                }
-                if (dyn && t == 0) {
-                    tthr = -0.5f * thr;
-                    S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
-                }
-            }
-            if (!ok) break;
-            merge_buffer<K, MB>(ks, kj, thr, cnt, mybuf, thr0);
-            S.thr_pub[wg][r] = make_uint2((uint32_t)vt, __float_as_uint(thr));
-            const int64_t row = pos < P.n_vox ? P.vperm[pos] : -1;
-            // Candidates above the other half's k-th best cannot be in the row's
-            // overall top-k; ks is ascending, so the rest is a prefix of length nv
-            // (a stale partner value only keeps more).
-            const uint2 pp = S.thr_pub[wg ^ 1][r];
-            const float cut = fminf(3.0e38f, pp.x == (uint32_t)vt ? __uint_as_float(pp.y) : 3.0e38f);
-            int nv = 0;
-#pragma unroll
-            for (int i = 0; i < K; ++i) nv += (ks[i] < 3.0e38f && ks[i] <= cut) ? 1 : 0;
-            // candidates (scan positions, ascending BF16 score) for the rescore kernel
-            if (row >= 0) {
-                int4* c = reinterpret_cast<int4*>(P.cand + (pos * EPI_WG + wg) * K);
-#pragma unroll
-                for (int i = 0; i < K; i += 4)
-                    c[i / 4] = make_int4(i < nv ? kj[i] : -1, i + 1 < nv ? kj[i + 1] : -1, i + 2 < nv ? kj[i + 2] : -1,
-                                         i + 3 < nv ? kj[i + 3] : -1);
-            }
-        }
+        epilogue_f<K, MODE>(S, P, tid, warp, lane, my_vt, tmem);
     }
     // ---- teardown: after an error, drain what the producer issued first ----
     fence_before();
